@@ -1,0 +1,332 @@
+/* C ABI of the GB300 tree-HMM accelerator (libthmm_gb300.so).
+ *
+ * This is the drop-in boundary for the reference's batched accelerator path,
+ * `tree_hmm::cuda` (include/tree_hmm/detail/gpu_backend_api.inc:1-142 and its
+ * implementation src/gpu_backend_impl.inc:1636-3130). Every entry point below
+ * names the reference declaration it replaces. The C++ API with the
+ * reference's exact types and overloads is the header-only layer
+ * include/tree_hmm/gb300.h, built on these functions.
+ *
+ * Conventions
+ *   - Plain pointers and sizes only. Floating-point buffers are `void *` in the
+ *     workspace's scalar width (THMM_SCALAR_F32 = float, THMM_SCALAR_F64 =
+ *     double), the reference's compile-time tree_hmm::Scalar.
+ *   - Every function returns a thmm_status. A non-zero status corresponds to
+ *     the C++ exception type the reference throws in the same situation; the
+ *     message is available from thmm_last_error() on the calling thread.
+ *   - Result pointers refer to workspace-owned pinned host memory and stay
+ *     valid until the workspace is reserved again or destroyed
+ *     (include/tree_hmm/accelerator.h:113-114).
+ *   - A workspace is not thread-safe; separate workspaces are independent.
+ *     Every call is synchronous, like the reference (src/gpu_backend_impl.inc:
+ *     2376), except thmm_enqueue.
+ */
+#ifndef THMM_GB300_H_
+#define THMM_GB300_H_
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum {
+  THMM_OK = 0,
+  THMM_INVALID_ARGUMENT = 1, /* std::invalid_argument */
+  THMM_LOGIC_ERROR = 2,      /* std::logic_error */
+  THMM_DOMAIN_ERROR = 3,     /* std::domain_error */
+  THMM_LENGTH_ERROR = 4,     /* std::length_error */
+  THMM_RUNTIME_ERROR = 5,    /* std::runtime_error (CUDA runtime failure) */
+} thmm_status;
+
+enum {
+  THMM_SCALAR_F32 = 4,
+  THMM_SCALAR_F64 = 8,
+};
+
+/* Reservation flags: which recovery tapes the workspace keeps
+ * (gpu_backend_api.inc:29-46). 0 reserves likelihood only. */
+enum {
+  THMM_RESERVE_MAXIMUM = 1u,
+  THMM_RESERVE_SAMPLING = 2u,
+  THMM_RESERVE_MARGINALS = 4u,
+  /* Extension: run the sum-product paths (partition, log partition,
+   * marginals) in FP64 instead of the default FP32 with exact power-of-two
+   * scaling. MAP and sampling always compute in the scalar width. */
+  THMM_COMPUTE_F64 = 0x100u,
+};
+
+/* tree_hmm::CategoricalInputUpdate (include/tree_hmm/accelerator.h:89-93). */
+enum {
+  THMM_UPDATE_ALL = 0,
+  THMM_UPDATE_FACTORS = 1,
+  THMM_UPDATE_NONE = 2,
+};
+
+/* Operations for thmm_enqueue. */
+enum {
+  THMM_OP_PARTITION = 0,
+  THMM_OP_LOG_PARTITION = 1,
+  THMM_OP_MAXIMUM = 2,
+  THMM_OP_SAMPLE = 3,
+  THMM_OP_MARGINALS = 4,
+};
+
+/* Message of the last failing call on this thread ("" if none). */
+const char *thmm_last_error(void);
+
+/* ---------------------------------------------------------------- plans -- */
+/* Opaque handle; in C++ it is exactly a btrc::Plan (include/btrc/plan.h). */
+typedef struct thmm_plan thmm_plan;
+
+typedef struct {
+  size_t num_nodes;
+  size_t num_edges;
+  size_t num_branches;
+  size_t num_compressions;
+  size_t num_combinations;
+  size_t num_absorptions;
+  size_t num_batches;
+  size_t num_rounds;
+  uint32_t root;
+} thmm_plan_info;
+
+/* Raw operation arrays of a plan; pointers stay valid while the plan lives.
+ * Layouts: rakes [n][4] (edge, leaf, branch, parent); combinations [n][3]
+ * (destination, source, parent); absorptions [n][3] (parent, branch, round);
+ * compressions [n][6] (left_edge, middle, right_edge, tape, parent, child);
+ * batches [n][3] (primitive 0..3, offset, count). */
+typedef struct {
+  const uint32_t *edge_parents;
+  const uint32_t *edge_children;
+  const uint32_t *rakes;
+  const uint32_t *combinations;
+  const uint32_t *absorptions;
+  const uint32_t *compressions;
+  const uint32_t *batches;
+} thmm_plan_arrays;
+
+/* btrc::MakePlan(parents) (consumed at tests/accelerator_test.h:19-20). */
+thmm_status thmm_plan_create(const int64_t *parents, size_t count,
+                             thmm_plan **out);
+void thmm_plan_destroy(thmm_plan *plan);
+thmm_status thmm_plan_get_info(const thmm_plan *plan, thmm_plan_info *out);
+thmm_status thmm_plan_get_arrays(const thmm_plan *plan, thmm_plan_arrays *out);
+
+/* -------------------------------------------------------------- devices -- */
+/* tree_hmm::cuda::Available() (gpu_backend_api.inc:1;
+ * src/gpu_backend_impl.inc:1779-1782). */
+int thmm_available(void);
+/* tree_hmm::cuda::DeviceDescription(device) (gpu_backend_api.inc:2;
+ * src/gpu_backend_impl.inc:1784-1797). Writes a NUL-terminated string. */
+thmm_status thmm_device_description(int device, char *buffer, size_t size);
+
+/* ----------------------------------------------------------- workspaces -- */
+typedef struct thmm_workspace thmm_workspace;
+
+/* Workspace() / ~Workspace() (gpu_backend_api.inc:4-14). */
+thmm_status thmm_workspace_create(thmm_workspace **out);
+void thmm_workspace_destroy(thmm_workspace *workspace);
+
+/* Reserve / ReserveMaximum / ReserveSampling / ReserveMarginals
+ * (gpu_backend_api.inc:17-21,29-31,36-37,43-44; src/gpu_backend_impl.inc:
+ * 1803-1966,2021-2063). `flags` selects the variant. */
+thmm_status thmm_reserve(thmm_workspace *workspace, const thmm_plan *plan,
+                         size_t states, size_t batch_capacity, int device,
+                         uint32_t flags, uint32_t scalar);
+
+/* ReserveCategorical and its Maximum / Sampling / Marginals variants
+ * (gpu_backend_api.inc:23-27,32-35,38-42,45-48; src/gpu_backend_impl.inc:
+ * 1978-2019). */
+thmm_status thmm_reserve_categorical(thmm_workspace *workspace,
+                                     const thmm_plan *plan, size_t states,
+                                     size_t batch_capacity, size_t categories,
+                                     const uint32_t *observation_nodes,
+                                     size_t observation_node_count, int device,
+                                     uint32_t flags, uint32_t scalar);
+
+/* Extension (no reference counterpart: the reference batch shares one
+ * topology, include/tree_hmm/accelerator.h:13-23). A forest of `tree_count`
+ * independent trees, each with its own plan and its own edge factors, run in
+ * one launch. Node and edge arrays are the per-tree arrays concatenated in
+ * tree order. */
+thmm_status thmm_reserve_forest(thmm_workspace *workspace,
+                                const thmm_plan *const *plans,
+                                size_t tree_count, size_t states, int device,
+                                uint32_t flags, uint32_t scalar);
+/* Categorical forest: `observation_nodes` holds each tree's strictly
+ * increasing observed nodes back to back, `observation_counts[t]` of them for
+ * tree t. The root and emission factors are shared by the forest. */
+thmm_status thmm_reserve_forest_categorical(
+    thmm_workspace *workspace, const thmm_plan *const *plans, size_t tree_count,
+    size_t states, size_t categories, const uint32_t *observation_nodes,
+    const size_t *observation_counts, int device, uint32_t flags,
+    uint32_t scalar);
+
+/* Pinned staging storage (Inputs / CategoricalInputs / Uniforms,
+ * gpu_backend_api.inc:52-59; src/gpu_backend_impl.inc:2065-2150).
+ * For a forest, `batch` must equal the tree count. */
+typedef struct {
+  size_t states;
+  size_t batch;
+  void *node_potentials; /* [batch, node, state] */
+  size_t node_count;
+  void *edge_potentials; /* [edge, parent, child] */
+  size_t edge_count;
+} thmm_dense_input_view;
+
+typedef struct {
+  size_t states;
+  size_t batch;
+  size_t categories;
+  const uint32_t *observation_nodes;
+  size_t observation_node_count;
+  uint8_t *observations; /* [batch, observation node] */
+  size_t observation_count;
+  void *root_potential; /* [state] */
+  size_t root_count;
+  void *emission_potentials; /* [category, state] */
+  size_t emission_count;
+  void *edge_potentials; /* [edge, parent, child] */
+  size_t edge_count;
+} thmm_categorical_input_view;
+
+thmm_status thmm_inputs(thmm_workspace *workspace, size_t batch,
+                        thmm_dense_input_view *out);
+thmm_status thmm_categorical_inputs(thmm_workspace *workspace, size_t batch,
+                                    thmm_categorical_input_view *out);
+thmm_status thmm_uniforms(thmm_workspace *workspace, size_t batch, void **out,
+                          size_t *count);
+
+/* tree_hmm::BatchedModelView (include/tree_hmm/accelerator.h:13-23). For a
+ * forest workspace `plan` is ignored and `batch` is the tree count. */
+typedef struct {
+  const thmm_plan *plan;
+  size_t states;
+  size_t batch;
+  const void *node_potentials;
+  size_t node_count;
+  const void *edge_potentials;
+  size_t edge_count;
+} thmm_dense_model;
+
+/* tree_hmm::BatchedCategoricalModelView (include/tree_hmm/accelerator.h:
+ * 41-58). */
+typedef struct {
+  const thmm_plan *plan;
+  size_t states;
+  size_t batch;
+  size_t categories;
+  const uint32_t *observation_nodes;
+  size_t observation_node_count;
+  const uint8_t *observations;
+  size_t observation_count;
+  const void *root_potential;
+  size_t root_count;
+  const void *emission_potentials;
+  size_t emission_count;
+  const void *edge_potentials;
+  size_t edge_count;
+} thmm_categorical_model;
+
+/* tree_hmm::AcceleratorTimings (include/tree_hmm/accelerator.h:98-111). */
+typedef struct {
+  double upload_ms;
+  double kernel_ms;
+  double download_ms;
+  double wall_ms;
+} thmm_timings;
+
+/* PartitionView (accelerator.h:115-118). */
+typedef struct {
+  const void *values;
+  size_t count;
+  thmm_timings timings;
+} thmm_partition_result;
+
+/* BatchedMaximumAssignmentView (accelerator.h:123-127). */
+typedef struct {
+  const void *log_weights;
+  size_t count;
+  const uint32_t *states;
+  size_t state_count;
+  thmm_timings timings;
+} thmm_maximum_result;
+
+/* BatchedPosteriorSampleView (accelerator.h:131-134). */
+typedef struct {
+  const uint32_t *states;
+  size_t count;
+  thmm_timings timings;
+} thmm_sample_result;
+
+/* BatchedMarginalView (accelerator.h:140-145). */
+typedef struct {
+  const void *log_partitions;
+  size_t count;
+  const void *nodes;
+  size_t node_count;
+  const void *edges;
+  size_t edge_count;
+  thmm_timings timings;
+} thmm_marginal_result;
+
+/* Dense prepared calls (gpu_backend_api.inc:97-99,103-104,110-111,117-119,
+ * 127-129; src/gpu_backend_impl.inc:3021-3118). */
+thmm_status thmm_partition_function(thmm_workspace *workspace,
+                                    const thmm_dense_model *model,
+                                    thmm_partition_result *out);
+thmm_status thmm_log_partition_function(thmm_workspace *workspace,
+                                        const thmm_dense_model *model,
+                                        thmm_partition_result *out);
+thmm_status thmm_maximum_a_posteriori(thmm_workspace *workspace,
+                                      const thmm_dense_model *model,
+                                      thmm_maximum_result *out);
+thmm_status thmm_posterior_sample(thmm_workspace *workspace,
+                                  const thmm_dense_model *model,
+                                  const void *uniforms, size_t uniform_count,
+                                  thmm_sample_result *out);
+thmm_status thmm_posterior_marginals(thmm_workspace *workspace,
+                                     const thmm_dense_model *model,
+                                     thmm_marginal_result *out);
+
+/* Categorical prepared calls with a CategoricalInputUpdate policy
+ * (gpu_backend_api.inc:100-102,105-109,112-116,120-126,130-142;
+ * src/gpu_backend_impl.inc:2842-2946). */
+thmm_status thmm_categorical_partition_function(
+    thmm_workspace *workspace, const thmm_categorical_model *model,
+    int update, thmm_partition_result *out);
+thmm_status thmm_categorical_log_partition_function(
+    thmm_workspace *workspace, const thmm_categorical_model *model,
+    int update, thmm_partition_result *out);
+thmm_status thmm_categorical_maximum_a_posteriori(
+    thmm_workspace *workspace, const thmm_categorical_model *model,
+    int update, thmm_maximum_result *out);
+thmm_status thmm_categorical_posterior_sample(
+    thmm_workspace *workspace, const thmm_categorical_model *model,
+    const void *uniforms, size_t uniform_count, int update,
+    thmm_sample_result *out);
+thmm_status thmm_categorical_posterior_marginals(
+    thmm_workspace *workspace, const thmm_categorical_model *model,
+    int update, thmm_marginal_result *out);
+
+/* Extension for device-resident timing and CUDA-graph capture (no reference
+ * counterpart). Enqueues only the device work of `operation` on the
+ * workspace stream, reading the inputs left resident by the previous prepared
+ * call of the same workspace; no host copies and no synchronisation.
+ * `nodes_out` (optional) receives the number of tree nodes processed. */
+thmm_status thmm_enqueue(thmm_workspace *workspace, int operation,
+                         uint64_t *nodes_out);
+/* The workspace's cudaStream_t, as an opaque pointer. */
+void *thmm_workspace_stream(thmm_workspace *workspace);
+thmm_status thmm_workspace_synchronize(thmm_workspace *workspace);
+
+/* Kernel launches made by the most recent prepared call or enqueue. */
+uint64_t thmm_workspace_launches(const thmm_workspace *workspace);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* THMM_GB300_H_ */

@@ -1,0 +1,96 @@
+"""In-tree build of libthmm_gb300.so (sm_103a) with nvcc.
+
+Each translation unit is compiled in parallel into parallel_tree_hmm_gb300/_build
+and linked into parallel_tree_hmm_gb300/libthmm_gb300.so. Only nvcc and the host
+C++ compiler are needed (no cmake, no torch extension machinery).
+"""
+from __future__ import annotations
+
+import concurrent.futures
+import os
+import pathlib
+import shutil
+import subprocess
+
+PACKAGE = pathlib.Path(__file__).resolve().parent
+ROOT = PACKAGE.parent
+CSRC = PACKAGE / "csrc"
+BUILD = PACKAGE / "_build"
+LIBRARY = PACKAGE / "libthmm_gb300.so"
+
+ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
+COMMON = [
+    "-std=c++20",
+    "-O3",
+    "-lineinfo",
+    "-Xcompiler",
+    "-fPIC",
+    "-Xcompiler",
+    "-ffp-contract=off",
+    f"-I{ROOT / 'include'}",
+    f"-I{CSRC}",
+]
+SOURCES = [
+    "btrc_plan.cc",
+    "program.cc",
+    "runtime.cc",
+    "engine_linear_f32.cu",
+    "engine_linear_f64.cu",
+    "engine_maximum.cu",
+    "engine_sample.cu",
+]
+
+
+def nvcc() -> str:
+    path = shutil.which("nvcc") or "/usr/local/cuda/bin/nvcc"
+    if not os.path.exists(path):
+        raise RuntimeError("nvcc not found; the CUDA toolkit is required")
+    return path
+
+
+def _compile(source: str) -> pathlib.Path:
+    src = CSRC / source
+    obj = BUILD / (source + ".o")
+    headers = list(CSRC.glob("*.h")) + list(CSRC.glob("*.cuh")) + list(
+        (ROOT / "include").rglob("*.h"))
+    newest = max([src.stat().st_mtime] + [h.stat().st_mtime for h in headers])
+    if obj.exists() and obj.stat().st_mtime >= newest:
+        return obj
+    cmd = [nvcc(), *COMMON, *ARCH, "-c", str(src), "-o", str(obj)]
+    if source.endswith(".cu"):
+        cmd[1:1] = ["-x", "cu"]
+    result = subprocess.run(cmd, capture_output=True, text=True)
+    if result.returncode != 0:
+        raise RuntimeError(f"nvcc failed for {source}:\n{result.stdout}\n{result.stderr}")
+    return obj
+
+
+def build_library(jobs: int | None = None) -> pathlib.Path:
+    BUILD.mkdir(exist_ok=True)
+    jobs = jobs or min(len(SOURCES), os.cpu_count() or 4)
+    with concurrent.futures.ThreadPoolExecutor(max_workers=jobs) as pool:
+        objects = list(pool.map(_compile, SOURCES))
+    if LIBRARY.exists() and LIBRARY.stat().st_mtime >= max(o.stat().st_mtime for o in objects):
+        return LIBRARY
+    tmp = LIBRARY.with_suffix(".so.tmp")
+    cmd = [nvcc(), *ARCH, "-shared", "-o", str(tmp), *map(str, objects)]
+    result = subprocess.run(cmd, capture_output=True, text=True)
+    if result.returncode != 0:
+        raise RuntimeError(f"link failed:\n{result.stdout}\n{result.stderr}")
+    os.replace(tmp, LIBRARY)
+    return LIBRARY
+
+
+def build_oracle(reference: bool = True) -> None:
+    """Builds the C oracle (test infrastructure) and, when the reference tree
+    is present, the reference CPU library and tests under oracle/_ref."""
+    oracle_dir = ROOT / "oracle"
+    subprocess.run(["make", "-s", "-C", str(oracle_dir)], check=True)
+    ref = os.environ.get("THMM_REFERENCE", "/root/reference")
+    if reference and os.path.isdir(os.path.join(ref, "src")):
+        subprocess.run(["make", "-s", "-C", str(oracle_dir), "ref", f"REF={ref}"], check=True)
+
+
+if __name__ == "__main__":
+    print(build_library())
+    build_oracle()

@@ -1,0 +1,15 @@
+// Sum-product kernels for float inputs/outputs (FP32 or FP64 arithmetic).
+#include "engine_launch.cuh"
+
+namespace thmm {
+
+cudaError_t LaunchLinearF32(bool compute_f64, unsigned kmax,
+                            const EngineArgs &args, int grid,
+                            cudaStream_t stream, int *blocks_per_sm) {
+  return compute_f64 ? LaunchLinearTyped<float, double>(kmax, args, grid, stream,
+                                                        blocks_per_sm)
+                     : LaunchLinearTyped<float, float>(kmax, args, grid, stream,
+                                                       blocks_per_sm);
+}
+
+} // namespace thmm

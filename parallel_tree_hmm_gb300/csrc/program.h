@@ -1,0 +1,63 @@
+// Host-side compilation of btrc plans into the device program format of
+// engine.h, and the kernel launch entry points implemented by the engine_*.cu
+// translation units.
+#ifndef THMM_PROGRAM_H_
+#define THMM_PROGRAM_H_
+
+#include <cstddef>
+#include <cstdint>
+#include <span>
+#include <vector>
+
+#include <cuda_runtime.h>
+
+#include "btrc/plan.h"
+#include "engine.h"
+
+namespace thmm {
+
+struct Uint2 {
+  std::uint32_t x, y;
+};
+struct Uint4 {
+  std::uint32_t x, y, z, w;
+};
+
+// Programs of every distinct plan of a workspace, concatenated.
+struct ProgramSet {
+  std::vector<DevProgram> programs;
+  std::vector<DevStep> steps;
+  std::vector<Uint4> rakes;
+  std::vector<Uint2> combines;
+  std::vector<Uint2> absorbs;
+  std::vector<Uint4> compress; // two entries per operation
+  std::vector<std::int32_t> obs_map;
+
+  // Appends the program of `plan`; `observation_nodes` (strictly increasing)
+  // builds the node -> observation-slot map when `categorical` is set.
+  std::uint32_t Add(const btrc::Plan &plan,
+                    std::span<const std::uint32_t> observation_nodes,
+                    bool categorical);
+};
+
+// Kernel entry points. `kmax` is the padded state count (4, 8, 16 or 32).
+// With `blocks_per_sm` non-null the call only reports the occupancy.
+cudaError_t LaunchLinearF32(bool compute_f64, unsigned kmax,
+                            const EngineArgs &args, int grid,
+                            cudaStream_t stream, int *blocks_per_sm);
+cudaError_t LaunchLinearF64(bool compute_f64, unsigned kmax,
+                            const EngineArgs &args, int grid,
+                            cudaStream_t stream, int *blocks_per_sm);
+cudaError_t LaunchMaximum(int scalar_bytes, unsigned kmax,
+                          const EngineArgs &args, int grid, cudaStream_t stream,
+                          int *blocks_per_sm);
+cudaError_t LaunchSample(int scalar_bytes, unsigned kmax, const EngineArgs &args,
+                         int grid, cudaStream_t stream, int *blocks_per_sm);
+
+inline unsigned PaddedStates(std::size_t states) {
+  return states <= 4 ? 4u : states <= 8 ? 8u : states <= 16 ? 16u : 32u;
+}
+
+} // namespace thmm
+
+#endif // THMM_PROGRAM_H_

@@ -1,0 +1,1206 @@
+// Host runtime of the accelerator: workspaces, staging, launch sequencing and
+// the C ABI declared in include/thmm_gb300.h.
+//
+// Behaviour follows the reference host driver (src/gpu_backend_impl.inc:
+// 1636-3130): one non-blocking stream and one device per workspace, pinned
+// staging buffers exposed through Inputs()/CategoricalInputs()/Uniforms(),
+// the kAll/kFactors/kNone residency rules for categorical inputs, six CUDA
+// events for the upload/kernel/download split plus a wall clock, and the same
+// exception classes (reported here as status codes). Where the reference
+// launches one kernel per primitive batch and phase, a prepared call here
+// launches one persistent kernel (engine.cuh) after a small memset.
+#include "thmm_gb300.h"
+
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <cstdlib>
+#include <cstdio>
+#include <cstring>
+#include <limits>
+#include <memory>
+#include <numeric>
+#include <stdexcept>
+#include <string>
+#include <unordered_map>
+#include <vector>
+
+#include <cuda_runtime.h>
+
+#include "btrc/plan.h"
+#include "engine.h"
+#include "program.h"
+
+struct thmm_plan; // a btrc::Plan in disguise
+
+namespace thmm {
+namespace {
+
+thread_local std::string g_last_error;
+using Clock = std::chrono::steady_clock;
+
+void Check(cudaError_t status, const char *what) {
+  if (status != cudaSuccess)
+    throw std::runtime_error(std::string(what) + ": " + cudaGetErrorString(status));
+}
+
+std::size_t CheckedProduct(std::initializer_list<std::size_t> values,
+                           const char *what) {
+  std::size_t result = 1;
+  for (const std::size_t value : values) {
+    if (value != 0 && result > std::numeric_limits<std::size_t>::max() / value)
+      throw std::length_error(std::string(what) + " overflows size_t");
+    result *= value;
+  }
+  return result;
+}
+
+const btrc::Plan &AsPlan(const thmm_plan *plan) {
+  if (plan == nullptr)
+    throw std::invalid_argument("plan must not be null");
+  return *reinterpret_cast<const btrc::Plan *>(plan);
+}
+
+// Raw device allocation owned by a workspace.
+struct DeviceBuffer {
+  void *ptr = nullptr;
+  std::size_t bytes = 0;
+  void Allocate(std::size_t size) {
+    Free();
+    Check(cudaMalloc(&ptr, std::max<std::size_t>(size, 16)), "cudaMalloc");
+    bytes = size;
+  }
+  void Free() noexcept {
+    if (ptr != nullptr)
+      static_cast<void>(cudaFree(ptr));
+    ptr = nullptr;
+    bytes = 0;
+  }
+  template <class T> T *as() const { return static_cast<T *>(ptr); }
+  template <class T> void Upload(const std::vector<T> &values, cudaStream_t stream) {
+    Allocate(values.size() * sizeof(T));
+    if (!values.empty())
+      Check(cudaMemcpyAsync(ptr, values.data(), values.size() * sizeof(T),
+                            cudaMemcpyHostToDevice, stream),
+            "cudaMemcpyAsync program upload");
+  }
+  ~DeviceBuffer() { Free(); }
+};
+
+struct HostBuffer {
+  void *ptr = nullptr;
+  std::size_t bytes = 0;
+  void Allocate(std::size_t size) {
+    Free();
+    Check(cudaMallocHost(&ptr, std::max<std::size_t>(size, 16)), "cudaMallocHost");
+    bytes = size;
+  }
+  void Free() noexcept {
+    if (ptr != nullptr)
+      static_cast<void>(cudaFreeHost(ptr));
+    ptr = nullptr;
+    bytes = 0;
+  }
+  template <class T> T *as() const { return static_cast<T *>(ptr); }
+  ~HostBuffer() { Free(); }
+};
+
+int TeamThreshold() {
+  if (const char *value = std::getenv("THMM_TEAM_THRESHOLD"))
+    return std::max(1, std::atoi(value));
+  return 2048;
+}
+
+} // namespace
+
+struct Workspace {
+  // Reservation.
+  bool reserved = false;
+  bool forest = false;
+  const btrc::Plan *plan = nullptr;
+  std::size_t states = 0;
+  std::size_t capacity = 0; // batch capacity, or tree count for a forest
+  int device = 0;
+  int scalar = THMM_SCALAR_F64;
+  bool compute_f64 = false;
+  bool maximum = false;
+  bool sampling = false;
+  bool marginals = false;
+  bool categorical = false;
+  std::size_t categories = 0;
+  std::vector<std::uint32_t> observation_nodes;
+  std::size_t resident_observation_batch = 0;
+  bool resident_factors = false;
+  std::size_t last_batch = 0;
+  bool has_run = false;
+  std::uint64_t launches = 0;
+
+  // Sizes for the full capacity.
+  std::size_t nodes_per_item = 0;     // batch API
+  std::size_t edges_per_item = 0;     // batch API
+  std::size_t observations_per_item = 0;
+  std::uint64_t total_nodes = 0;      // all instances
+  std::uint64_t total_edges_out = 0;  // all instances
+  std::uint64_t edge_inputs = 0;      // matrices in the edge input
+  std::uint64_t total_observations = 0;
+  std::vector<std::uint64_t> tree_nodes; // forest: per tree
+
+  // Device program.
+  DeviceBuffer programs, steps, rakes, combines, absorbs, compress, instances;
+  DeviceBuffer big_items, small_items, obs_map, control;
+  std::uint32_t big_count = 0;
+  std::uint32_t small_count = 0;
+  bool items_big = false;
+
+  // Device data.
+  DeviceBuffer node_in, edge_in, observations, root_potential, emission;
+  DeviceBuffer uniforms, values, node_out, edge_out, states_out, scratch, bytes;
+
+  // Pinned staging.
+  HostBuffer h_node_in, h_edge_in, h_observations, h_root, h_emission;
+  HostBuffer h_uniforms, h_values, h_node_out, h_edge_out, h_states, h_control;
+
+  cudaStream_t stream = nullptr;
+  cudaEvent_t events[6] = {};
+  int sms = 1;
+  int occupancy[3] = {1, 1, 1};
+
+  ~Workspace() { Clear(); }
+
+  void Clear() noexcept {
+    if (stream != nullptr) {
+      static_cast<void>(cudaSetDevice(device));
+      static_cast<void>(cudaStreamSynchronize(stream));
+    }
+    for (DeviceBuffer *buffer :
+         {&programs, &steps, &rakes, &combines, &absorbs, &compress, &instances,
+          &big_items, &small_items, &obs_map, &control, &node_in, &edge_in,
+          &observations, &root_potential, &emission, &uniforms, &values,
+          &node_out, &edge_out, &states_out, &scratch, &bytes})
+      buffer->Free();
+    for (HostBuffer *buffer :
+         {&h_node_in, &h_edge_in, &h_observations, &h_root, &h_emission,
+          &h_uniforms, &h_values, &h_node_out, &h_edge_out, &h_states,
+          &h_control})
+      buffer->Free();
+    for (cudaEvent_t &event : events) {
+      if (event != nullptr)
+        static_cast<void>(cudaEventDestroy(event));
+      event = nullptr;
+    }
+    if (stream != nullptr)
+      static_cast<void>(cudaStreamDestroy(stream));
+    stream = nullptr;
+    reserved = forest = false;
+    plan = nullptr;
+    states = capacity = 0;
+    maximum = sampling = marginals = categorical = false;
+    categories = 0;
+    observation_nodes.clear();
+    tree_nodes.clear();
+    resident_observation_batch = 0;
+    resident_factors = false;
+    last_batch = 0;
+    has_run = false;
+  }
+
+  std::size_t ScalarBytes() const { return static_cast<std::size_t>(scalar); }
+
+  // ---------------------------------------------------------------- reserve
+  // Common part of every Reserve* (src/gpu_backend_impl.inc:1803-1870).
+  void Begin(std::size_t state_count, int device_index, std::uint32_t flags,
+             std::uint32_t scalar_bytes) {
+    if (scalar_bytes != THMM_SCALAR_F32 && scalar_bytes != THMM_SCALAR_F64)
+      throw std::invalid_argument("scalar width must be 4 or 8 bytes");
+    if (state_count == 0)
+      throw std::invalid_argument(
+          "accelerator state and batch counts must be nonzero");
+    if (state_count > 32)
+      throw std::invalid_argument(
+          "state count exceeds the accelerator compression block limit");
+    Clear();
+    device = device_index;
+    Check(cudaSetDevice(device), "cudaSetDevice");
+    Check(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device),
+          "cudaDeviceGetAttribute");
+    Check(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking),
+          "cudaStreamCreateWithFlags");
+    for (cudaEvent_t &event : events)
+      Check(cudaEventCreate(&event), "cudaEventCreate");
+    states = state_count;
+    scalar = static_cast<int>(scalar_bytes);
+    compute_f64 = (flags & THMM_COMPUTE_F64) != 0;
+    maximum = (flags & THMM_RESERVE_MAXIMUM) != 0;
+    sampling = (flags & THMM_RESERVE_SAMPLING) != 0;
+    marginals = (flags & THMM_RESERVE_MARGINALS) != 0;
+  }
+
+  // Builds programs, instances, work queues and buffers for `plans[i]`
+  // applied to instance i.
+  void Build(const std::vector<const btrc::Plan *> &instance_plans,
+             const std::vector<std::vector<std::uint32_t>> &instance_observations,
+             bool shared_edges) {
+    ProgramSet set;
+    std::unordered_map<const btrc::Plan *, std::uint32_t> program_of;
+    const std::size_t count = instance_plans.size();
+    std::vector<DevInstance> table(count);
+    const std::uint64_t K = states;
+    const std::uint64_t KK = K * K;
+    std::uint64_t node_base = 0, edge_base = 0, obs_base = 0;
+    std::uint64_t scratch_base = 0, byte_base = 0;
+    const std::size_t compute_bytes =
+        std::max<std::size_t>(ScalarBytes(), compute_f64 ? 8 : 4);
+    for (std::size_t i = 0; i < count; ++i) {
+      const btrc::Plan &p = *instance_plans[i];
+      std::uint32_t program;
+      const auto found = program_of.find(&p);
+      if (found != program_of.end() && !categorical) {
+        program = found->second;
+      } else if (found != program_of.end() && shared_edges) {
+        program = found->second; // batch API: one plan, one observation set
+      } else {
+        program = set.Add(p, instance_observations.empty()
+                                 ? std::span<const std::uint32_t>()
+                                 : std::span<const std::uint32_t>(
+                                       instance_observations[i]),
+                          categorical);
+        program_of[&p] = program;
+      }
+      DevInstance &instance = table[i];
+      instance.program = program;
+      instance.node_base = node_base;
+      instance.edge_in_base = shared_edges ? 0 : edge_base;
+      instance.edge_out_base = edge_base;
+      instance.obs_base = obs_base;
+      // Scratch: the largest layout among the reserved operations.
+      ScratchSize size = InstanceScratch(p.num_nodes(), p.num_branches(),
+                                         p.num_compressions(), K, kModeLinear,
+                                         marginals);
+      if (maximum) {
+        const ScratchSize m = InstanceScratch(p.num_nodes(), p.num_branches(),
+                                              p.num_compressions(), K,
+                                              kModeMaximum, false);
+        size.elements = std::max(size.elements, m.elements);
+        size.bytes = std::max(size.bytes, m.bytes);
+      }
+      instance.scratch_base = scratch_base;
+      instance.byte_base = byte_base;
+      scratch_base += size.elements;
+      byte_base += size.bytes;
+      node_base += p.num_nodes();
+      edge_base += p.num_edges();
+      obs_base += instance_observations.empty() ? 0
+                  : instance_observations[i].size();
+      tree_nodes.push_back(p.num_nodes());
+    }
+    total_nodes = node_base;
+    total_edges_out = edge_base;
+    edge_inputs = shared_edges ? instance_plans.front()->num_edges() : edge_base;
+    total_observations = obs_base;
+
+    // Work queues: large instances go to whole-CTA teams, small ones to
+    // single-warp teams; both ordered largest first.
+    const std::uint64_t threshold = static_cast<std::uint64_t>(TeamThreshold());
+    std::vector<std::uint32_t> order(count);
+    std::iota(order.begin(), order.end(), 0u);
+    std::stable_sort(order.begin(), order.end(), [&](std::uint32_t a, std::uint32_t b) {
+      return tree_nodes[a] > tree_nodes[b];
+    });
+    std::vector<std::uint32_t> big, small;
+    for (const std::uint32_t i : order)
+      (tree_nodes[i] >= threshold ? big : small).push_back(i);
+    big_count = static_cast<std::uint32_t>(big.size());
+    small_count = static_cast<std::uint32_t>(small.size());
+    items_big = !big.empty();
+
+    programs.Upload(set.programs, stream);
+    steps.Upload(set.steps, stream);
+    rakes.Upload(set.rakes, stream);
+    combines.Upload(set.combines, stream);
+    absorbs.Upload(set.absorbs, stream);
+    compress.Upload(set.compress, stream);
+    obs_map.Upload(set.obs_map, stream);
+    instances.Upload(table, stream);
+    big_items.Upload(big, stream);
+    small_items.Upload(small, stream);
+    control.Allocate(16);
+
+    // Inputs, outputs and scratch.
+    const std::size_t S = ScalarBytes();
+    const std::uint64_t edge_values = edge_inputs * KK;
+    if (!categorical) {
+      node_in.Allocate(total_nodes * K * S);
+      h_node_in.Allocate(total_nodes * K * S);
+    } else {
+      observations.Allocate(total_observations);
+      h_observations.Allocate(total_observations);
+      root_potential.Allocate(K * S);
+      h_root.Allocate(K * S);
+      emission.Allocate(categories * K * S);
+      h_emission.Allocate(categories * K * S);
+    }
+    edge_in.Allocate(edge_values * S);
+    h_edge_in.Allocate(edge_values * S);
+    values.Allocate(count * S);
+    h_values.Allocate(count * S);
+    h_control.Allocate(16);
+    if (marginals) {
+      node_out.Allocate(total_nodes * K * S);
+      h_node_out.Allocate(total_nodes * K * S);
+      edge_out.Allocate(total_edges_out * KK * S);
+      h_edge_out.Allocate(total_edges_out * KK * S);
+    }
+    if (maximum || sampling) {
+      states_out.Allocate(total_nodes * sizeof(std::uint32_t));
+      h_states.Allocate(total_nodes * sizeof(std::uint32_t));
+    }
+    if (sampling) {
+      uniforms.Allocate(total_nodes * S);
+      h_uniforms.Allocate(total_nodes * S);
+    }
+    scratch.Allocate(scratch_base * compute_bytes);
+    bytes.Allocate(byte_base);
+
+    // Occupancy of each kernel this workspace may launch.
+    const unsigned kmax = PaddedStates(states);
+    EngineArgs probe{};
+    occupancy[0] = occupancy[1] = occupancy[2] = 1;
+    Check(scalar == 8 ? LaunchLinearF64(compute_f64, kmax, probe, 0, nullptr, &occupancy[0])
+                      : LaunchLinearF32(compute_f64, kmax, probe, 0, nullptr, &occupancy[0]),
+          "occupancy query");
+    if (maximum)
+      Check(LaunchMaximum(scalar, kmax, probe, 0, nullptr, &occupancy[1]),
+            "occupancy query");
+    if (sampling)
+      Check(LaunchSample(scalar, kmax, probe, 0, nullptr, &occupancy[2]),
+            "occupancy query");
+    Check(cudaStreamSynchronize(stream), "topology upload");
+    reserved = true;
+  }
+
+  void ReserveBatch(const btrc::Plan &p, std::size_t state_count,
+                    std::size_t batch, int device_index, std::uint32_t flags,
+                    std::uint32_t scalar_bytes, bool is_categorical,
+                    std::size_t category_count,
+                    std::span<const std::uint32_t> observed) {
+    if (is_categorical) {
+      if (category_count == 0 || category_count > 256)
+        throw std::invalid_argument("accelerator categorical model must have "
+                                    "between 1 and 256 categories");
+      ValidateObservationNodes(p, observed);
+    }
+    if (batch == 0)
+      throw std::invalid_argument(
+          "accelerator state and batch counts must be nonzero");
+    Begin(state_count, device_index, flags, scalar_bytes);
+    plan = &p;
+    capacity = batch;
+    categorical = is_categorical;
+    categories = category_count;
+    observation_nodes.assign(observed.begin(), observed.end());
+    nodes_per_item = p.num_nodes();
+    edges_per_item = p.num_edges();
+    observations_per_item = observed.size();
+    CheckedProduct({batch, p.num_nodes(), state_count}, "node workspace");
+    CheckedProduct({batch, p.num_edges(), state_count, state_count},
+                   "edge workspace");
+    std::vector<const btrc::Plan *> instance_plans(batch, &p);
+    std::vector<std::vector<std::uint32_t>> instance_observations;
+    if (categorical)
+      instance_observations.assign(batch, observation_nodes);
+    Build(instance_plans, instance_observations, true);
+  }
+
+  void ReserveForest(std::span<const btrc::Plan *const> plans,
+                     std::size_t state_count, int device_index,
+                     std::uint32_t flags, std::uint32_t scalar_bytes,
+                     bool is_categorical, std::size_t category_count,
+                     const std::uint32_t *observed, const std::size_t *counts) {
+    if (plans.empty())
+      throw std::invalid_argument("a forest needs at least one tree");
+    for (const btrc::Plan *p : plans)
+      if (p == nullptr)
+        throw std::invalid_argument("forest plan must not be null");
+    std::vector<std::vector<std::uint32_t>> instance_observations;
+    if (is_categorical) {
+      if (category_count == 0 || category_count > 256)
+        throw std::invalid_argument("accelerator categorical model must have "
+                                    "between 1 and 256 categories");
+      std::size_t offset = 0;
+      for (std::size_t t = 0; t < plans.size(); ++t) {
+        const std::size_t n = counts == nullptr ? 0 : counts[t];
+        const std::span<const std::uint32_t> tree_observed(
+            observed == nullptr ? nullptr : observed + offset, n);
+        ValidateObservationNodes(*plans[t], tree_observed);
+        instance_observations.emplace_back(tree_observed.begin(),
+                                           tree_observed.end());
+        offset += n;
+      }
+    }
+    Begin(state_count, device_index, flags, scalar_bytes);
+    forest = true;
+    capacity = plans.size();
+    categorical = is_categorical;
+    categories = category_count;
+    for (const auto &tree : instance_observations)
+      observation_nodes.insert(observation_nodes.end(), tree.begin(), tree.end());
+    Build(std::vector<const btrc::Plan *>(plans.begin(), plans.end()),
+          instance_observations, false);
+  }
+
+  static void ValidateObservationNodes(const btrc::Plan &p,
+                                       std::span<const std::uint32_t> observed) {
+    for (std::size_t i = 0; i < observed.size(); ++i) {
+      if (observed[i] >= p.num_nodes() || (i > 0 && observed[i] <= observed[i - 1]))
+        throw std::invalid_argument(
+            "accelerator categorical observation nodes must be valid and "
+            "strictly increasing");
+    }
+  }
+
+  // ----------------------------------------------------------- staging views
+  void RequireReserved() const {
+    if (!reserved)
+      throw std::logic_error("accelerator Workspace::Reserve must precede Inputs");
+  }
+
+  std::size_t NodesFor(std::size_t batch) const {
+    return forest ? total_nodes : batch * nodes_per_item;
+  }
+  std::size_t EdgeOutFor(std::size_t batch) const {
+    return forest ? total_edges_out : batch * edges_per_item;
+  }
+  std::size_t ObservationsFor(std::size_t batch) const {
+    return forest ? total_observations : batch * observations_per_item;
+  }
+  void CheckBatch(std::size_t batch, const char *what) const {
+    if (forest ? batch != capacity : (batch == 0 || batch > capacity))
+      throw std::invalid_argument(std::string("accelerator ") + what +
+                                  " batch exceeds the reserved capacity");
+  }
+
+  // ------------------------------------------------------------------- run
+  struct Upload {
+    const void *source;
+    HostBuffer *staging;
+    DeviceBuffer *device;
+    std::size_t bytes;
+  };
+
+  void EnqueueDevice(int operation, std::size_t batch) {
+    const unsigned kmax = PaddedStates(states);
+    EngineArgs args{};
+    args.programs = programs.as<DevProgram>();
+    args.steps = steps.as<DevStep>();
+    args.rakes = rakes.ptr;
+    args.combines = combines.ptr;
+    args.absorbs = absorbs.ptr;
+    args.compress = compress.ptr;
+    args.instances = instances.as<DevInstance>();
+    args.big_items = big_items.as<std::uint32_t>();
+    args.small_items = small_items.as<std::uint32_t>();
+    if (forest) {
+      args.big_count = big_count;
+      args.small_count = small_count;
+    } else {
+      args.big_count = items_big ? static_cast<std::uint32_t>(batch) : 0u;
+      args.small_count = items_big ? 0u : static_cast<std::uint32_t>(batch);
+    }
+    args.queue = control.as<std::uint32_t>();
+    args.error = control.as<std::uint32_t>() + 2;
+    args.node_in = node_in.ptr;
+    args.observations = observations.as<std::uint8_t>();
+    args.obs_map = obs_map.as<std::int32_t>();
+    args.root_potential = root_potential.ptr;
+    args.emission = emission.ptr;
+    args.categories = static_cast<std::uint32_t>(categories);
+    args.categorical = categorical ? 1u : 0u;
+    args.edge_in = edge_in.ptr;
+    args.states = static_cast<std::uint32_t>(states);
+    args.reverse = operation == THMM_OP_MARGINALS ? 1u : 0u;
+    args.raw = operation == THMM_OP_PARTITION ? 1u : 0u;
+    args.scratch = scratch.ptr;
+    args.bytes = bytes.as<std::uint8_t>();
+    args.values = values.ptr;
+    args.node_out = node_out.ptr;
+    args.edge_out = edge_out.ptr;
+    args.states_out = states_out.as<std::uint32_t>();
+    args.uniforms = uniforms.ptr;
+
+    const int kind = operation == THMM_OP_MAXIMUM ? 1
+                     : operation == THMM_OP_SAMPLE ? 2
+                                                   : 0;
+    const std::uint64_t teams_needed =
+        std::max<std::uint64_t>(args.big_count, (args.small_count + kWarpsPerCta - 1) /
+                                                    kWarpsPerCta);
+    const int grid = static_cast<int>(std::max<std::uint64_t>(
+        1, std::min<std::uint64_t>(teams_needed,
+                                   static_cast<std::uint64_t>(sms) *
+                                       std::max(occupancy[kind], 1))));
+    Check(cudaMemsetAsync(control.ptr, 0, 16, stream), "cudaMemsetAsync");
+    cudaError_t status;
+    if (kind == 1)
+      status = LaunchMaximum(scalar, kmax, args, grid, stream, nullptr);
+    else if (kind == 2)
+      status = LaunchSample(scalar, kmax, args, grid, stream, nullptr);
+    else if (scalar == 8)
+      status = LaunchLinearF64(compute_f64, kmax, args, grid, stream, nullptr);
+    else
+      status = LaunchLinearF32(compute_f64, kmax, args, grid, stream, nullptr);
+    Check(status, "tree-HMM accelerator kernel launch");
+    launches = 1;
+  }
+
+  struct Outcome {
+    thmm_timings timings;
+    std::uint32_t error;
+  };
+
+  Outcome Run(int operation, std::size_t batch, const std::vector<Upload> &uploads,
+              Clock::time_point wall_start) {
+    Check(cudaSetDevice(device), "cudaSetDevice");
+    for (const Upload &upload : uploads)
+      if (upload.source != upload.staging->ptr && upload.bytes != 0)
+        std::memcpy(upload.staging->ptr, upload.source, upload.bytes);
+    Check(cudaEventRecord(events[0], stream), "cudaEventRecord");
+    for (const Upload &upload : uploads)
+      if (upload.bytes != 0)
+        Check(cudaMemcpyAsync(upload.device->ptr, upload.staging->ptr, upload.bytes,
+                              cudaMemcpyHostToDevice, stream),
+              "cudaMemcpyAsync input upload");
+    Check(cudaEventRecord(events[1], stream), "cudaEventRecord");
+    Check(cudaEventRecord(events[2], stream), "cudaEventRecord");
+    EnqueueDevice(operation, batch);
+    Check(cudaEventRecord(events[3], stream), "cudaEventRecord");
+    Check(cudaEventRecord(events[4], stream), "cudaEventRecord");
+    const std::size_t S = ScalarBytes();
+    const std::size_t items = forest ? capacity : batch;
+    const auto download = [&](HostBuffer &host, DeviceBuffer &dev, std::size_t n) {
+      if (n != 0)
+        Check(cudaMemcpyAsync(host.ptr, dev.ptr, n, cudaMemcpyDeviceToHost, stream),
+              "cudaMemcpyAsync result download");
+    };
+    download(h_values, values, items * S);
+    download(h_control, control, 16);
+    if (operation == THMM_OP_MARGINALS) {
+      download(h_node_out, node_out, NodesFor(batch) * states * S);
+      download(h_edge_out, edge_out, EdgeOutFor(batch) * states * states * S);
+    }
+    if (operation == THMM_OP_MAXIMUM || operation == THMM_OP_SAMPLE)
+      download(h_states, states_out, NodesFor(batch) * sizeof(std::uint32_t));
+    Check(cudaEventRecord(events[5], stream), "cudaEventRecord");
+    Check(cudaEventSynchronize(events[5]), "tree-HMM accelerator execution");
+    last_batch = batch;
+    has_run = true;
+    float upload_ms = 0, kernel_ms = 0, download_ms = 0;
+    Check(cudaEventElapsedTime(&upload_ms, events[0], events[1]), "cudaEventElapsedTime");
+    Check(cudaEventElapsedTime(&kernel_ms, events[2], events[3]), "cudaEventElapsedTime");
+    Check(cudaEventElapsedTime(&download_ms, events[4], events[5]), "cudaEventElapsedTime");
+    Outcome outcome{};
+    outcome.timings.upload_ms = upload_ms;
+    outcome.timings.kernel_ms = kernel_ms;
+    outcome.timings.download_ms = download_ms;
+    outcome.error = h_control.as<std::uint32_t>()[2];
+    outcome.timings.wall_ms =
+        std::chrono::duration<double, std::milli>(Clock::now() - wall_start).count();
+    return outcome;
+  }
+
+  double Value(std::size_t index) const {
+    return scalar == 8 ? h_values.as<double>()[index]
+                       : static_cast<double>(h_values.as<float>()[index]);
+  }
+
+  void RequireAllFinite(std::size_t count, const char *message) const {
+    for (std::size_t i = 0; i < count; ++i)
+      if (!std::isfinite(Value(i)))
+        throw std::domain_error(message);
+  }
+
+  static constexpr int kWarpsPerCta = 4;
+};
+
+namespace {
+
+template <class Body> thmm_status Guard(Body body) {
+  try {
+    body();
+    g_last_error.clear();
+    return THMM_OK;
+  } catch (const std::invalid_argument &error) {
+    g_last_error = error.what();
+    return THMM_INVALID_ARGUMENT;
+  } catch (const std::domain_error &error) {
+    g_last_error = error.what();
+    return THMM_DOMAIN_ERROR;
+  } catch (const std::length_error &error) {
+    g_last_error = error.what();
+    return THMM_LENGTH_ERROR;
+  } catch (const std::logic_error &error) {
+    g_last_error = error.what();
+    return THMM_LOGIC_ERROR;
+  } catch (const std::bad_alloc &) {
+    g_last_error = "host allocation failed";
+    return THMM_RUNTIME_ERROR;
+  } catch (const std::exception &error) {
+    g_last_error = error.what();
+    return THMM_RUNTIME_ERROR;
+  }
+}
+
+Workspace &AsWorkspace(thmm_workspace *workspace) {
+  if (workspace == nullptr)
+    throw std::invalid_argument("workspace must not be null");
+  return *reinterpret_cast<Workspace *>(workspace);
+}
+
+// Shape and reservation checks shared by the dense calls
+// (src/gpu_backend_impl.inc:2162-2187,2809-2818).
+void CheckDense(const Workspace &ws, const thmm_dense_model &model,
+                const char *requirement, bool reserved_for_operation) {
+  if (!ws.reserved)
+    throw std::invalid_argument(requirement);
+  if (ws.categorical)
+    throw std::invalid_argument(
+        "dense accelerator inference cannot use a categorical workspace");
+  if ((!ws.forest && reinterpret_cast<const btrc::Plan *>(model.plan) != ws.plan) ||
+      model.states != ws.states || !reserved_for_operation)
+    throw std::invalid_argument(requirement);
+  ws.CheckBatch(model.batch, "input");
+  if (model.node_count != ws.NodesFor(model.batch) * ws.states ||
+      (model.node_count != 0 && model.node_potentials == nullptr))
+    throw std::invalid_argument("accelerator node input shape is wrong");
+  if (model.edge_count != ws.edge_inputs * ws.states * ws.states ||
+      (model.edge_count != 0 && model.edge_potentials == nullptr))
+    throw std::invalid_argument("accelerator edge input shape is wrong");
+}
+
+std::vector<Workspace::Upload> DenseUploads(Workspace &ws,
+                                            const thmm_dense_model &model) {
+  const std::size_t S = ws.ScalarBytes();
+  return {{model.node_potentials, &ws.h_node_in, &ws.node_in, model.node_count * S},
+          {model.edge_potentials, &ws.h_edge_in, &ws.edge_in, model.edge_count * S}};
+}
+
+// Categorical checks and residency rules (src/gpu_backend_impl.inc:2842-2946).
+std::vector<Workspace::Upload> CategoricalUploads(Workspace &ws,
+                                                  const thmm_categorical_model &model,
+                                                  int update,
+                                                  const char *requirement,
+                                                  bool reserved_for_operation) {
+  if (!ws.reserved || !ws.categorical || model.categories != ws.categories ||
+      model.observation_node_count != ws.observation_nodes.size() ||
+      (model.observation_node_count != 0 &&
+       (model.observation_nodes == nullptr ||
+        !std::equal(model.observation_nodes,
+                    model.observation_nodes + model.observation_node_count,
+                    ws.observation_nodes.begin()))))
+    throw std::invalid_argument(
+        "categorical accelerator model does not match the reserved workspace");
+  if (update != THMM_UPDATE_ALL && update != THMM_UPDATE_FACTORS &&
+      update != THMM_UPDATE_NONE)
+    throw std::invalid_argument("unknown categorical input update policy");
+  if ((!ws.forest && reinterpret_cast<const btrc::Plan *>(model.plan) != ws.plan) ||
+      model.states != ws.states || !reserved_for_operation)
+    throw std::invalid_argument(requirement);
+  ws.CheckBatch(model.batch, "categorical input");
+  if (model.observation_count != ws.ObservationsFor(model.batch) ||
+      model.root_count != ws.states ||
+      model.emission_count != ws.categories * ws.states ||
+      (model.observation_count != 0 && model.observations == nullptr) ||
+      model.root_potential == nullptr || model.emission_potentials == nullptr)
+    throw std::invalid_argument("accelerator categorical input shapes are wrong");
+  if (model.edge_count != ws.edge_inputs * ws.states * ws.states ||
+      (model.edge_count != 0 && model.edge_potentials == nullptr))
+    throw std::invalid_argument("accelerator edge input shape is wrong");
+  const bool update_observations = update == THMM_UPDATE_ALL;
+  const bool update_factors = update != THMM_UPDATE_NONE;
+  if (!update_observations && ws.resident_observation_batch != model.batch)
+    throw std::logic_error(
+        "categorical observations are not resident for this batch; use kAll");
+  if (!update_factors && !ws.resident_factors)
+    throw std::logic_error(
+        "categorical factors are not resident; use kAll or kFactors");
+  const std::size_t S = ws.ScalarBytes();
+  std::vector<Workspace::Upload> uploads;
+  if (update_observations)
+    uploads.push_back({model.observations, &ws.h_observations, &ws.observations,
+                       model.observation_count});
+  if (update_factors) {
+    uploads.push_back({model.root_potential, &ws.h_root, &ws.root_potential,
+                       model.root_count * S});
+    uploads.push_back({model.emission_potentials, &ws.h_emission, &ws.emission,
+                       model.emission_count * S});
+    uploads.push_back({model.edge_potentials, &ws.h_edge_in, &ws.edge_in,
+                       model.edge_count * S});
+  }
+  return uploads;
+}
+
+void MarkResident(Workspace &ws, std::size_t batch, int update) {
+  if (update == THMM_UPDATE_ALL)
+    ws.resident_observation_batch = batch;
+  if (update != THMM_UPDATE_NONE)
+    ws.resident_factors = true;
+}
+
+std::vector<Workspace::Upload> UniformUpload(Workspace &ws, std::size_t batch,
+                                             const void *uniforms,
+                                             std::size_t count) {
+  if (count != ws.NodesFor(batch) || (count != 0 && uniforms == nullptr))
+    throw std::invalid_argument(
+        "prepared accelerator posterior sampling requires ReserveSampling and "
+        "one uniform variate per batch item and node");
+  return {{uniforms, &ws.h_uniforms, &ws.uniforms, count * ws.ScalarBytes()}};
+}
+
+void CheckSamplingOutcome(const Workspace &ws, const Workspace::Outcome &outcome,
+                          std::size_t items) {
+  if (outcome.error & kErrorInvalidUniform)
+    throw std::invalid_argument("posterior-sampling variates must lie in [0, 1)");
+  ws.RequireAllFinite(items, "the tree HMM has a nonpositive partition function");
+  if (outcome.error & kErrorEmptyConditional)
+    throw std::domain_error("cannot sample from an empty conditional distribution");
+}
+
+constexpr const char *kReserveMessage =
+    "prepared accelerator inference requires Workspace::Reserve for this plan, "
+    "state count, and batch capacity";
+constexpr const char *kReserveMaximumMessage =
+    "prepared accelerator MAP inference requires ReserveMaximum for this plan, "
+    "state count, and batch capacity";
+constexpr const char *kReserveSamplingMessage =
+    "prepared accelerator posterior sampling requires ReserveSampling and one "
+    "uniform variate per batch item and node";
+constexpr const char *kReserveMarginalsMessage =
+    "prepared accelerator marginal inference requires ReserveMarginals for "
+    "this plan, state count, and batch capacity";
+
+} // namespace
+} // namespace thmm
+
+using thmm::Guard;
+using thmm::Workspace;
+
+// ======================================================================= C ABI
+extern "C" {
+
+const char *thmm_last_error(void) { return thmm::g_last_error.c_str(); }
+
+thmm_status thmm_plan_create(const int64_t *parents, size_t count,
+                             thmm_plan **out) {
+  return Guard([&] {
+    if (out == nullptr || (count != 0 && parents == nullptr))
+      throw std::invalid_argument("plan arguments must not be null");
+    auto plan = std::make_unique<btrc::Plan>(
+        btrc::MakePlan(std::span<const std::int64_t>(parents, count)));
+    *out = reinterpret_cast<thmm_plan *>(plan.release());
+  });
+}
+
+void thmm_plan_destroy(thmm_plan *plan) {
+  delete reinterpret_cast<btrc::Plan *>(plan);
+}
+
+thmm_status thmm_plan_get_info(const thmm_plan *plan, thmm_plan_info *out) {
+  return Guard([&] {
+    const btrc::Plan &p = thmm::AsPlan(plan);
+    if (out == nullptr)
+      throw std::invalid_argument("output must not be null");
+    *out = {p.num_nodes(),
+            p.num_edges(),
+            p.num_branches(),
+            p.num_compressions(),
+            p.branch_combinations().size(),
+            p.branch_absorptions().size(),
+            p.primitive_batches().size(),
+            p.rounds().size(),
+            p.root()};
+  });
+}
+
+thmm_status thmm_plan_get_arrays(const thmm_plan *plan, thmm_plan_arrays *out) {
+  return Guard([&] {
+    const btrc::Plan &p = thmm::AsPlan(plan);
+    if (out == nullptr)
+      throw std::invalid_argument("output must not be null");
+    static_assert(sizeof(btrc::PrimitiveBatch) == 12);
+    out->edge_parents = p.edge_parents().data();
+    out->edge_children = p.edge_children().data();
+    out->rakes = reinterpret_cast<const uint32_t *>(p.rakes().data());
+    out->combinations =
+        reinterpret_cast<const uint32_t *>(p.branch_combinations().data());
+    out->absorptions =
+        reinterpret_cast<const uint32_t *>(p.branch_absorptions().data());
+    out->compressions = reinterpret_cast<const uint32_t *>(p.compressions().data());
+    out->batches = reinterpret_cast<const uint32_t *>(p.primitive_batches().data());
+  });
+}
+
+int thmm_available(void) {
+  int count = 0;
+  return cudaGetDeviceCount(&count) == cudaSuccess && count > 0 ? 1 : 0;
+}
+
+thmm_status thmm_device_description(int device, char *buffer, size_t size) {
+  return Guard([&] {
+    cudaDeviceProp properties{};
+    thmm::Check(cudaGetDeviceProperties(&properties, device),
+                "cudaGetDeviceProperties");
+    const std::string text = std::string(properties.name) + " (compute " +
+                             std::to_string(properties.major) + "." +
+                             std::to_string(properties.minor) + ")";
+    if (buffer == nullptr || size == 0)
+      throw std::invalid_argument("description buffer must not be empty");
+    std::snprintf(buffer, size, "%s", text.c_str());
+  });
+}
+
+thmm_status thmm_workspace_create(thmm_workspace **out) {
+  return Guard([&] {
+    if (out == nullptr)
+      throw std::invalid_argument("output must not be null");
+    *out = reinterpret_cast<thmm_workspace *>(new Workspace());
+  });
+}
+
+void thmm_workspace_destroy(thmm_workspace *workspace) {
+  delete reinterpret_cast<Workspace *>(workspace);
+}
+
+thmm_status thmm_reserve(thmm_workspace *workspace, const thmm_plan *plan,
+                         size_t states, size_t batch_capacity, int device,
+                         uint32_t flags, uint32_t scalar) {
+  return Guard([&] {
+    thmm::AsWorkspace(workspace).ReserveBatch(thmm::AsPlan(plan), states,
+                                              batch_capacity, device, flags,
+                                              scalar, false, 0, {});
+  });
+}
+
+thmm_status thmm_reserve_categorical(thmm_workspace *workspace,
+                                     const thmm_plan *plan, size_t states,
+                                     size_t batch_capacity, size_t categories,
+                                     const uint32_t *observation_nodes,
+                                     size_t observation_node_count, int device,
+                                     uint32_t flags, uint32_t scalar) {
+  return Guard([&] {
+    if (observation_node_count != 0 && observation_nodes == nullptr)
+      throw std::invalid_argument("observation nodes must not be null");
+    thmm::AsWorkspace(workspace).ReserveBatch(
+        thmm::AsPlan(plan), states, batch_capacity, device, flags, scalar, true,
+        categories,
+        std::span<const std::uint32_t>(observation_nodes, observation_node_count));
+  });
+}
+
+thmm_status thmm_reserve_forest(thmm_workspace *workspace,
+                                const thmm_plan *const *plans,
+                                size_t tree_count, size_t states, int device,
+                                uint32_t flags, uint32_t scalar) {
+  return Guard([&] {
+    if (plans == nullptr)
+      throw std::invalid_argument("forest plans must not be null");
+    thmm::AsWorkspace(workspace).ReserveForest(
+        std::span<const btrc::Plan *const>(
+            reinterpret_cast<const btrc::Plan *const *>(plans), tree_count),
+        states, device, flags, scalar, false, 0, nullptr, nullptr);
+  });
+}
+
+thmm_status thmm_reserve_forest_categorical(
+    thmm_workspace *workspace, const thmm_plan *const *plans, size_t tree_count,
+    size_t states, size_t categories, const uint32_t *observation_nodes,
+    const size_t *observation_counts, int device, uint32_t flags,
+    uint32_t scalar) {
+  return Guard([&] {
+    if (plans == nullptr || observation_counts == nullptr)
+      throw std::invalid_argument("forest arrays must not be null");
+    thmm::AsWorkspace(workspace).ReserveForest(
+        std::span<const btrc::Plan *const>(
+            reinterpret_cast<const btrc::Plan *const *>(plans), tree_count),
+        states, device, flags, scalar, true, categories, observation_nodes,
+        observation_counts);
+  });
+}
+
+thmm_status thmm_inputs(thmm_workspace *workspace, size_t batch,
+                        thmm_dense_input_view *out) {
+  return Guard([&] {
+    Workspace &ws = thmm::AsWorkspace(workspace);
+    ws.RequireReserved();
+    if (ws.categorical)
+      throw std::logic_error(
+          "accelerator dense Inputs cannot be used after ReserveCategorical");
+    ws.CheckBatch(batch, "input");
+    *out = {ws.states,
+            batch,
+            ws.h_node_in.ptr,
+            ws.NodesFor(batch) * ws.states,
+            ws.h_edge_in.ptr,
+            static_cast<size_t>(ws.edge_inputs * ws.states * ws.states)};
+  });
+}
+
+thmm_status thmm_categorical_inputs(thmm_workspace *workspace, size_t batch,
+                                    thmm_categorical_input_view *out) {
+  return Guard([&] {
+    Workspace &ws = thmm::AsWorkspace(workspace);
+    if (!ws.reserved || !ws.categorical)
+      throw std::logic_error("accelerator Workspace::ReserveCategorical must "
+                             "precede CategoricalInputs");
+    ws.CheckBatch(batch, "categorical input");
+    *out = {ws.states,
+            batch,
+            ws.categories,
+            ws.observation_nodes.data(),
+            ws.observation_nodes.size(),
+            ws.h_observations.as<uint8_t>(),
+            ws.ObservationsFor(batch),
+            ws.h_root.ptr,
+            ws.states,
+            ws.h_emission.ptr,
+            ws.categories * ws.states,
+            ws.h_edge_in.ptr,
+            static_cast<size_t>(ws.edge_inputs * ws.states * ws.states)};
+  });
+}
+
+thmm_status thmm_uniforms(thmm_workspace *workspace, size_t batch, void **out,
+                          size_t *count) {
+  return Guard([&] {
+    Workspace &ws = thmm::AsWorkspace(workspace);
+    if (!ws.reserved || !ws.sampling)
+      throw std::logic_error(
+          "accelerator Workspace::ReserveSampling must precede Uniforms");
+    ws.CheckBatch(batch, "uniform");
+    *out = ws.h_uniforms.ptr;
+    *count = ws.NodesFor(batch);
+  });
+}
+
+// ------------------------------------------------------------ dense calls
+static thmm_status DensePartition(thmm_workspace *workspace,
+                                  const thmm_dense_model *model, int operation,
+                                  thmm_partition_result *out) {
+  const auto wall_start = thmm::Clock::now();
+  return Guard([&] {
+    Workspace &ws = thmm::AsWorkspace(workspace);
+    if (model == nullptr || out == nullptr)
+      throw std::invalid_argument("model and result must not be null");
+    thmm::CheckDense(ws, *model, thmm::kReserveMessage, true);
+    const auto outcome = ws.Run(operation, model->batch,
+                                thmm::DenseUploads(ws, *model), wall_start);
+    *out = {ws.h_values.ptr, ws.forest ? ws.capacity : model->batch, outcome.timings};
+  });
+}
+
+thmm_status thmm_partition_function(thmm_workspace *workspace,
+                                    const thmm_dense_model *model,
+                                    thmm_partition_result *out) {
+  return DensePartition(workspace, model, THMM_OP_PARTITION, out);
+}
+
+thmm_status thmm_log_partition_function(thmm_workspace *workspace,
+                                        const thmm_dense_model *model,
+                                        thmm_partition_result *out) {
+  return DensePartition(workspace, model, THMM_OP_LOG_PARTITION, out);
+}
+
+thmm_status thmm_maximum_a_posteriori(thmm_workspace *workspace,
+                                      const thmm_dense_model *model,
+                                      thmm_maximum_result *out) {
+  const auto wall_start = thmm::Clock::now();
+  return Guard([&] {
+    Workspace &ws = thmm::AsWorkspace(workspace);
+    if (model == nullptr || out == nullptr)
+      throw std::invalid_argument("model and result must not be null");
+    thmm::CheckDense(ws, *model, thmm::kReserveMaximumMessage, ws.maximum);
+    const auto outcome = ws.Run(THMM_OP_MAXIMUM, model->batch,
+                                thmm::DenseUploads(ws, *model), wall_start);
+    const std::size_t items = ws.forest ? ws.capacity : model->batch;
+    ws.RequireAllFinite(items, "the tree HMM has no positive-weight assignment");
+    *out = {ws.h_values.ptr, items, ws.h_states.as<uint32_t>(),
+            ws.NodesFor(model->batch), outcome.timings};
+  });
+}
+
+thmm_status thmm_posterior_sample(thmm_workspace *workspace,
+                                  const thmm_dense_model *model,
+                                  const void *uniforms, size_t uniform_count,
+                                  thmm_sample_result *out) {
+  const auto wall_start = thmm::Clock::now();
+  return Guard([&] {
+    Workspace &ws = thmm::AsWorkspace(workspace);
+    if (model == nullptr || out == nullptr)
+      throw std::invalid_argument("model and result must not be null");
+    thmm::CheckDense(ws, *model, thmm::kReserveSamplingMessage, ws.sampling);
+    auto uploads = thmm::DenseUploads(ws, *model);
+    const auto uniform = thmm::UniformUpload(ws, model->batch, uniforms, uniform_count);
+    uploads.insert(uploads.end(), uniform.begin(), uniform.end());
+    const auto outcome = ws.Run(THMM_OP_SAMPLE, model->batch, uploads, wall_start);
+    const std::size_t items = ws.forest ? ws.capacity : model->batch;
+    thmm::CheckSamplingOutcome(ws, outcome, items);
+    *out = {ws.h_states.as<uint32_t>(), ws.NodesFor(model->batch), outcome.timings};
+  });
+}
+
+thmm_status thmm_posterior_marginals(thmm_workspace *workspace,
+                                     const thmm_dense_model *model,
+                                     thmm_marginal_result *out) {
+  const auto wall_start = thmm::Clock::now();
+  return Guard([&] {
+    Workspace &ws = thmm::AsWorkspace(workspace);
+    if (model == nullptr || out == nullptr)
+      throw std::invalid_argument("model and result must not be null");
+    thmm::CheckDense(ws, *model, thmm::kReserveMarginalsMessage, ws.marginals);
+    const auto outcome = ws.Run(THMM_OP_MARGINALS, model->batch,
+                                thmm::DenseUploads(ws, *model), wall_start);
+    const std::size_t items = ws.forest ? ws.capacity : model->batch;
+    ws.RequireAllFinite(items, "the tree HMM has a nonpositive partition function");
+    *out = {ws.h_values.ptr,
+            items,
+            ws.h_node_out.ptr,
+            ws.NodesFor(model->batch) * ws.states,
+            ws.h_edge_out.ptr,
+            ws.EdgeOutFor(model->batch) * ws.states * ws.states,
+            outcome.timings};
+  });
+}
+
+// ------------------------------------------------------ categorical calls
+static thmm_status CategoricalPartition(thmm_workspace *workspace,
+                                        const thmm_categorical_model *model,
+                                        int update, int operation,
+                                        thmm_partition_result *out) {
+  const auto wall_start = thmm::Clock::now();
+  return Guard([&] {
+    Workspace &ws = thmm::AsWorkspace(workspace);
+    if (model == nullptr || out == nullptr)
+      throw std::invalid_argument("model and result must not be null");
+    const auto uploads =
+        thmm::CategoricalUploads(ws, *model, update, thmm::kReserveMessage, true);
+    const auto outcome = ws.Run(operation, model->batch, uploads, wall_start);
+    thmm::MarkResident(ws, model->batch, update);
+    *out = {ws.h_values.ptr, ws.forest ? ws.capacity : model->batch, outcome.timings};
+  });
+}
+
+thmm_status thmm_categorical_partition_function(
+    thmm_workspace *workspace, const thmm_categorical_model *model, int update,
+    thmm_partition_result *out) {
+  return CategoricalPartition(workspace, model, update, THMM_OP_PARTITION, out);
+}
+
+thmm_status thmm_categorical_log_partition_function(
+    thmm_workspace *workspace, const thmm_categorical_model *model, int update,
+    thmm_partition_result *out) {
+  return CategoricalPartition(workspace, model, update, THMM_OP_LOG_PARTITION, out);
+}
+
+thmm_status thmm_categorical_maximum_a_posteriori(
+    thmm_workspace *workspace, const thmm_categorical_model *model, int update,
+    thmm_maximum_result *out) {
+  const auto wall_start = thmm::Clock::now();
+  return Guard([&] {
+    Workspace &ws = thmm::AsWorkspace(workspace);
+    if (model == nullptr || out == nullptr)
+      throw std::invalid_argument("model and result must not be null");
+    const auto uploads = thmm::CategoricalUploads(
+        ws, *model, update, thmm::kReserveMaximumMessage, ws.maximum);
+    const auto outcome = ws.Run(THMM_OP_MAXIMUM, model->batch, uploads, wall_start);
+    const std::size_t items = ws.forest ? ws.capacity : model->batch;
+    ws.RequireAllFinite(items, "the tree HMM has no positive-weight assignment");
+    thmm::MarkResident(ws, model->batch, update);
+    *out = {ws.h_values.ptr, items, ws.h_states.as<uint32_t>(),
+            ws.NodesFor(model->batch), outcome.timings};
+  });
+}
+
+thmm_status thmm_categorical_posterior_sample(
+    thmm_workspace *workspace, const thmm_categorical_model *model,
+    const void *uniforms, size_t uniform_count, int update,
+    thmm_sample_result *out) {
+  const auto wall_start = thmm::Clock::now();
+  return Guard([&] {
+    Workspace &ws = thmm::AsWorkspace(workspace);
+    if (model == nullptr || out == nullptr)
+      throw std::invalid_argument("model and result must not be null");
+    auto uploads = thmm::CategoricalUploads(
+        ws, *model, update, thmm::kReserveSamplingMessage, ws.sampling);
+    const auto uniform = thmm::UniformUpload(ws, model->batch, uniforms, uniform_count);
+    uploads.insert(uploads.end(), uniform.begin(), uniform.end());
+    const auto outcome = ws.Run(THMM_OP_SAMPLE, model->batch, uploads, wall_start);
+    const std::size_t items = ws.forest ? ws.capacity : model->batch;
+    thmm::CheckSamplingOutcome(ws, outcome, items);
+    thmm::MarkResident(ws, model->batch, update);
+    *out = {ws.h_states.as<uint32_t>(), ws.NodesFor(model->batch), outcome.timings};
+  });
+}
+
+thmm_status thmm_categorical_posterior_marginals(
+    thmm_workspace *workspace, const thmm_categorical_model *model, int update,
+    thmm_marginal_result *out) {
+  const auto wall_start = thmm::Clock::now();
+  return Guard([&] {
+    Workspace &ws = thmm::AsWorkspace(workspace);
+    if (model == nullptr || out == nullptr)
+      throw std::invalid_argument("model and result must not be null");
+    const auto uploads = thmm::CategoricalUploads(
+        ws, *model, update, thmm::kReserveMarginalsMessage, ws.marginals);
+    const auto outcome = ws.Run(THMM_OP_MARGINALS, model->batch, uploads, wall_start);
+    const std::size_t items = ws.forest ? ws.capacity : model->batch;
+    ws.RequireAllFinite(items, "the tree HMM has a nonpositive partition function");
+    thmm::MarkResident(ws, model->batch, update);
+    *out = {ws.h_values.ptr,
+            items,
+            ws.h_node_out.ptr,
+            ws.NodesFor(model->batch) * ws.states,
+            ws.h_edge_out.ptr,
+            ws.EdgeOutFor(model->batch) * ws.states * ws.states,
+            outcome.timings};
+  });
+}
+
+// ------------------------------------------------------- device-only path
+thmm_status thmm_enqueue(thmm_workspace *workspace, int operation,
+                         uint64_t *nodes_out) {
+  return Guard([&] {
+    Workspace &ws = thmm::AsWorkspace(workspace);
+    if (!ws.reserved || !ws.has_run)
+      throw std::logic_error(
+          "thmm_enqueue needs inputs left resident by a prepared call");
+    if (operation < THMM_OP_PARTITION || operation > THMM_OP_MARGINALS)
+      throw std::invalid_argument("unknown operation");
+    if ((operation == THMM_OP_MAXIMUM && !ws.maximum) ||
+        (operation == THMM_OP_SAMPLE && !ws.sampling) ||
+        (operation == THMM_OP_MARGINALS && !ws.marginals))
+      throw std::invalid_argument("operation was not reserved");
+    thmm::Check(cudaSetDevice(ws.device), "cudaSetDevice");
+    ws.EnqueueDevice(operation, ws.last_batch);
+    if (nodes_out != nullptr)
+      *nodes_out = ws.NodesFor(ws.last_batch);
+  });
+}
+
+void *thmm_workspace_stream(thmm_workspace *workspace) {
+  return workspace == nullptr
+             ? nullptr
+             : static_cast<void *>(reinterpret_cast<Workspace *>(workspace)->stream);
+}
+
+thmm_status thmm_workspace_synchronize(thmm_workspace *workspace) {
+  return Guard([&] {
+    Workspace &ws = thmm::AsWorkspace(workspace);
+    if (ws.stream != nullptr)
+      thmm::Check(cudaStreamSynchronize(ws.stream), "cudaStreamSynchronize");
+  });
+}
+
+uint64_t thmm_workspace_launches(const thmm_workspace *workspace) {
+  return workspace == nullptr
+             ? 0
+             : reinterpret_cast<const Workspace *>(workspace)->launches;
+}
+
+} // extern "C"
