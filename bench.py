@@ -1,0 +1,436 @@
+"""Benchmark: batched posterior marginals (log Z + node/edge marginals, the
+gradient of log Z) over an uneven forest, on GB300.
+
+Workload (one step = one categorical kFactors call over the whole forest):
+4096 trees with node counts log-uniform in [200, 20000], half random recursive
+trees, half caterpillars; K = 4 states (--states 20 for the larger variant);
+row-stochastic Dirichlet(0.5) edge factors, every leaf observed with a byte
+uniform over K categories, Dirichlet(1) root factor and emission rows. Inputs
+are seeded synthetic data. The edge factors of one step (1.1 GB at K = 4)
+exceed the 129 MB L2, so no flush is needed between timed steps.
+
+Reported:
+  value       device-resident throughput, tree nodes/s: the persistent kernel
+              re-run on inputs already in HBM, CUDA events on the workspace
+              stream.
+  e2e         the same metric through the C ABI prepared call with pinned host
+              buffers: upload of the step's edge/root/emission factors, kernel,
+              download of log Z and all node and edge marginals.
+  roofline    algorithmic bytes per launch / launch time against the measured
+              HBM copy bandwidth.
+  cpu_baseline  the oracle port of the reference FP64 CPU path on a bounded
+              sample of the same forest, all host cores.
+  config.plain_fp64_*  the same kernel with FP64 arithmetic (the plain FP64
+              form) on the same inputs.
+
+`--impl reference` times the reference CPU algorithm (oracle port, FP64, all
+host cores) on the same workload instead.
+"""
+from __future__ import annotations
+
+import argparse
+import concurrent.futures
+import json
+import math
+import os
+import pathlib
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = pathlib.Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+METRIC = "tree-nodes/s for logZ+marginals+grad"
+UNIT = "nodes/s"
+
+
+def parse_args():
+    parser = argparse.ArgumentParser()
+    parser.add_argument("--gpus", type=int, default=1)
+    parser.add_argument("--steps", type=int, default=20)
+    parser.add_argument("--warmup", type=int, default=3)
+    parser.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    parser.add_argument("--states", type=int, default=4)
+    parser.add_argument("--trees", type=int, default=4096)
+    parser.add_argument("--seed", type=int, default=0)
+    parser.add_argument("--e2e-steps", type=int, default=None)
+    parser.add_argument("--cpu-sample-nodes", type=int, default=8_000_000)
+    return parser.parse_args()
+
+
+# ------------------------------------------------------------------ workload
+class Forest:
+    def __init__(self, trees: int, states: int, seed: int):
+        from parallel_tree_hmm_gb300 import synthetic
+
+        rng = np.random.default_rng(seed)
+        sizes = np.exp(rng.uniform(math.log(200), math.log(20000), size=trees))
+        sizes = np.maximum(2, np.round(sizes).astype(np.int64))
+        self.parents = []
+        for index, n in enumerate(sizes):
+            if index % 2 == 0:
+                self.parents.append(synthetic.random_recursive(rng, int(n)))
+            else:
+                self.parents.append(synthetic.caterpillar(int(n)))
+        self.states = states
+        self.observed = [synthetic.leaves(p) for p in self.parents]
+        self.num_nodes = np.array([len(p) for p in self.parents], dtype=np.int64)
+        self.total_nodes = int(self.num_nodes.sum())
+        self.total_edges = int((self.num_nodes - 1).sum())
+        self.total_observed = int(sum(len(o) for o in self.observed))
+        self.rng = rng
+
+    def factors(self, seed: int):
+        """One kFactors draw: root, emission and edge factors (float32)."""
+        from parallel_tree_hmm_gb300 import synthetic
+
+        rng = np.random.default_rng(seed)
+        K = self.states
+        root = synthetic.dirichlet_rows(rng, 1, K, 1.0, np.float32).ravel()
+        emission = synthetic.dirichlet_rows(rng, K, K, 1.0, np.float32).ravel()
+        g = rng.standard_gamma(0.5, size=(self.total_edges * K, K), dtype=np.float32)
+        g /= g.sum(axis=1, keepdims=True)
+        np.nan_to_num(g, copy=False, nan=1.0 / K)
+        return root, emission, g.ravel()
+
+    def observations(self):
+        return self.rng.integers(0, self.states, size=self.total_observed,
+                                 dtype=np.uint8)
+
+    def algorithmic_bytes(self, scalar_bytes: int = 4) -> int:
+        """Compulsory bytes of one marginal launch: edge factors in, one byte
+        per observation in, node marginals, edge marginals and log Z out."""
+        K = self.states
+        return (self.total_edges * K * K * scalar_bytes * 2
+                + self.total_observed
+                + self.total_nodes * K * scalar_bytes
+                + len(self.parents) * scalar_bytes
+                + (K + K * K) * scalar_bytes)
+
+
+# -------------------------------------------------------------------- clocks
+class ClockSampler:
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int):
+        self.device = device
+        self.process = None
+        self.lines = []
+        self.thread = None
+
+    def __enter__(self):
+        try:
+            self.process = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.device}", f"--query-gpu={self.FIELDS}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except (OSError, FileNotFoundError):
+            self.process = None
+        return self
+
+    def _read(self):
+        for line in self.process.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *exc):
+        if self.process is not None:
+            self.process.terminate()
+            try:
+                self.process.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.process.kill()
+        if self.thread is not None:
+            self.thread.join(timeout=5)
+
+    def summary(self):
+        sm, max_sm, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown",
+                 "sw_power_cap"]
+        for line in self.lines:
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                max_sm = float(parts[2])
+            except ValueError:
+                continue
+            for name, flag in zip(names, parts[5:9]):
+                if flag.lower() == "active":
+                    reasons.add(name)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unavailable"],
+                    "samples": 0}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max_sm,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+# ---------------------------------------------------------------- CPU leg
+def cpu_baseline(forest: Forest, root, emission, edges, observations, sample_nodes):
+    """Reference FP64 CPU marginals (oracle port) on the first trees of the
+    forest whose node count reaches `sample_nodes`, over all host cores."""
+    import parallel_tree_hmm_gb300 as thmm
+    from oracle import bridge
+
+    K = forest.states
+    edge_offsets = np.concatenate([[0], np.cumsum(forest.num_nodes - 1)])
+    obs_offsets = np.concatenate([[0], np.cumsum([len(o) for o in forest.observed])])
+    chosen, nodes_total = [], 0
+    for t in range(len(forest.parents)):
+        chosen.append(t)
+        nodes_total += int(forest.num_nodes[t])
+        if nodes_total >= sample_nodes:
+            break
+    emission64 = emission.astype(np.float64).reshape(K, K)
+    root64 = root.astype(np.float64)
+    jobs = []
+    for t in chosen:
+        parents = forest.parents[t]
+        dense = np.ones((len(parents), K))
+        dense[0] = root64
+        obs = observations[obs_offsets[t]:obs_offsets[t + 1]]
+        dense[forest.observed[t]] *= emission64[obs]
+        tree_edges = edges[edge_offsets[t] * K * K:edge_offsets[t + 1] * K * K]
+        jobs.append((thmm.Plan(parents), dense.ravel(), tree_edges.astype(np.float64)))
+    cores = os.cpu_count() or 1
+
+    def run(job):
+        plan, dense, tree_edges = job
+        return bridge.marginals(plan, K, dense, tree_edges)[0]
+
+    start = time.perf_counter()
+    with concurrent.futures.ThreadPoolExecutor(max_workers=cores) as pool:
+        list(pool.map(run, jobs))
+    elapsed = time.perf_counter() - start
+    return {"value": nodes_total / elapsed, "unit": UNIT, "cores": cores, "kind": "port",
+            "sample": f"first {len(chosen)} trees ({nodes_total} nodes) of the forest, "
+                      f"FP64 log-domain marginals, {elapsed:.2f} s"}
+
+
+# ------------------------------------------------------------------- main
+def main():
+    args = parse_args()
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local_rank = int(os.environ.get("LOCAL_RANK", "0"))
+    dist = None
+    if world > 1:
+        import torch.distributed as dist  # noqa: F811
+
+        import torch
+        torch.cuda.set_device(local_rank)
+        dist.init_process_group("nccl" if args.impl == "ours" else "gloo")
+
+    if args.impl == "reference":
+        run_reference(args, rank, world, dist)
+    else:
+        run_ours(args, rank, world, local_rank, dist)
+    if dist is not None:
+        dist.barrier()
+        dist.destroy_process_group()
+
+
+def reduce_max(value, dist):
+    if dist is None:
+        return value
+    import torch
+
+    tensor = torch.tensor([value], dtype=torch.float64,
+                          device="cuda" if torch.cuda.is_available() else "cpu")
+    dist.all_reduce(tensor, op=dist.ReduceOp.MAX)
+    return float(tensor.item())
+
+
+def run_reference(args, rank, world, dist):
+    if rank != 0:
+        return
+    forest = Forest(args.trees, args.states, args.seed)
+    root, emission, edges = forest.factors(args.seed + 1)
+    observations = forest.observations()
+    sample = max(200_000, args.cpu_sample_nodes // 4)
+    for _ in range(args.warmup):
+        cpu_baseline(forest, root, emission, edges, observations, sample // 4)
+    values = []
+    for _ in range(args.steps):
+        values.append(cpu_baseline(forest, root, emission, edges, observations, sample))
+    value = statistics.median(v["value"] for v in values)
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT,
+        "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": None, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": workload_config(args, forest),
+        "cpu_baseline": {**values[-1], "value": value},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def workload_config(args, forest):
+    return {
+        "workload": (f"uneven forest: {len(forest.parents)} trees, nodes log-uniform "
+                     f"[200, 20000], half random recursive / half caterpillar, "
+                     f"K={forest.states}, categorical leaves, kFactors posterior marginals"),
+        "trees": len(forest.parents), "nodes_per_rank": forest.total_nodes,
+        "edges_per_rank": forest.total_edges, "states": forest.states,
+        "seed": args.seed, "parallelism": f"replicas of the forest per GPU x{args.gpus}",
+        "l2": "inputs larger than L2 (edge factors of one step > 129 MB)",
+    }
+
+
+def run_ours(args, rank, world, local_rank, dist):
+    import torch
+
+    import parallel_tree_hmm_gb300 as thmm
+
+    device = local_rank
+    torch.cuda.set_device(device)
+    forest = Forest(args.trees, args.states, args.seed + 1000 * rank)
+    K = forest.states
+    plans = [thmm.Plan(p) for p in forest.parents]
+    factor_sets = [forest.factors(args.seed + 1 + i + 1000 * rank) for i in range(2)]
+    observations = forest.observations()
+
+    def reserve(compute):
+        ws = thmm.Workspace()
+        ws.reserve_forest_categorical(plans, K, K, forest.observed, device, kind="marginals",
+                                      scalar=np.float32, compute=compute)
+        return ws
+
+    def stage(ws, factors):
+        staged = ws.categorical_inputs()
+        root, emission, edges = factors
+        staged.root_potential[:] = root
+        staged.emission_potentials[:] = emission
+        staged.edge_potentials[:] = edges
+        return staged
+
+    ws = reserve(np.float32)
+    staged = stage(ws, factor_sets[0])
+    staged.observations[:] = observations
+    first = ws.posterior_marginals_prepared(staged, thmm.CategoricalInputUpdate.kAll)
+    if not np.all(np.isfinite(first.log_partitions)):
+        raise RuntimeError("non-finite log partition in the benchmark workload")
+    log_z_reference = first.log_partitions.copy()
+    node_sum = first.nodes.reshape(-1, K).sum(axis=1)
+    normalisation_error = float(np.max(np.abs(node_sum - 1.0)))
+
+    stream = torch.cuda.ExternalStream(ws.stream, device=device)
+
+    def device_time(workspace, steps, warmup, sampler=None):
+        ext = torch.cuda.ExternalStream(workspace.stream, device=device)
+        for _ in range(warmup):
+            workspace.enqueue(4)
+        torch.cuda.synchronize(device)
+        if dist is not None:
+            dist.barrier()
+        torch.cuda.synchronize(device)
+        start = torch.cuda.Event(enable_timing=True)
+        stop = torch.cuda.Event(enable_timing=True)
+        start.record(ext)
+        nodes = 0
+        for _ in range(steps):
+            nodes += workspace.enqueue(4)
+        stop.record(ext)
+        stop.synchronize()
+        torch.cuda.synchronize(device)
+        if dist is not None:
+            dist.barrier()
+        return start.elapsed_time(stop), nodes
+
+    sampler = ClockSampler(device)
+    with sampler:
+        elapsed_ms, nodes_done = device_time(ws, args.steps, args.warmup)
+    elapsed_ms = reduce_max(elapsed_ms, dist)
+    launch_ms = elapsed_ms / args.steps
+    value = nodes_done * world / (elapsed_ms / 1e3)
+
+    # Plain FP64 arithmetic on the same inputs.
+    ws64 = reserve(np.float64)
+    staged64 = stage(ws64, factor_sets[0])
+    staged64.observations[:] = observations
+    plain = ws64.posterior_marginals_prepared(staged64, thmm.CategoricalInputUpdate.kAll)
+    plain_logz_diff = float(np.max(np.abs(plain.log_partitions.astype(np.float64)
+                                          - log_z_reference.astype(np.float64))
+                                   / np.maximum(1.0, np.abs(plain.log_partitions))))
+    plain_steps = max(2, args.steps // 4)
+    plain_ms, plain_nodes = device_time(ws64, plain_steps, 1)
+    plain_value = plain_nodes * world / (reduce_max(plain_ms, dist) / 1e3)
+    del ws64, staged64, plain
+
+    # End to end through the prepared call: pinned staging -> H2D -> kernel -> D2H.
+    e2e_steps = args.e2e_steps or max(3, min(args.steps, 10))
+    for i in range(args.warmup):
+        stage(ws, factor_sets[i % 2])
+        ws.posterior_marginals_prepared(staged, thmm.CategoricalInputUpdate.kFactors)
+    e2e_total = 0.0
+    api_kernel_ms = []
+    for i in range(e2e_steps):
+        stage(ws, factor_sets[i % 2])
+        torch.cuda.synchronize(device)
+        if dist is not None:
+            dist.barrier()
+        begin = time.perf_counter()
+        result = ws.posterior_marginals_prepared(staged, thmm.CategoricalInputUpdate.kFactors)
+        e2e_total += time.perf_counter() - begin
+        api_kernel_ms.append(result.timings.kernel_ms)
+    e2e_total = reduce_max(e2e_total, dist)
+    e2e_value = forest.total_nodes * world * e2e_steps / e2e_total
+    S = 4
+    h2d = forest.total_edges * K * K * S + (K + K * K) * S
+    d2h = len(plans) * S + forest.total_nodes * K * S + forest.total_edges * K * K * S + 16
+
+    algorithmic = forest.algorithmic_bytes()
+    peaks = json.loads((ROOT / "MEASURED_PEAKS.json").read_text()) \
+        if (ROOT / "MEASURED_PEAKS.json").exists() else {}
+    peak = peaks.get("hbm_gbs", 6800.0)
+    achieved = algorithmic / (launch_ms / 1e3) / 1e9
+    traffic = None
+    traffic_file = ROOT / "profiles" / "engine_traffic.json"
+    if traffic_file.exists():
+        info = json.loads(traffic_file.read_text())
+        key = f"K{K}"
+        if key in info:
+            traffic = info[key]["bytes_per_node"] * forest.total_nodes
+
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": launch_ms,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32", "data": "synthetic",
+        "config": {**workload_config(args, forest),
+                   "plain_fp64_nodes_per_s": plain_value,
+                   "chosen_over_plain_fp64": value / plain_value,
+                   "plain_fp64_log_z_rel_diff": plain_logz_diff,
+                   "node_marginal_normalisation_error": normalisation_error},
+        "roofline": {"bound": "hbm", "achieved": achieved,
+                     "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                     "peak_source": "measured" if peaks else "fallback",
+                     "traffic": traffic,
+                     "algorithmic_bytes_per_launch": algorithmic},
+        "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d,
+                "d2h_bytes_per_step": d2h,
+                "api_kernel_ms_median": statistics.median(api_kernel_ms)},
+        "gpu_launches": args.steps,
+        "clocks": sampler.summary(),
+    }
+    if rank == 0 and world == 1 and args.cpu_sample_nodes > 0:
+        root, emission, edges = factor_sets[0]
+        line["cpu_baseline"] = cpu_baseline(forest, root, emission, edges, observations,
+                                            args.cpu_sample_nodes)
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+
+
+if __name__ == "__main__":
+    main()

@@ -98,20 +98,28 @@ class Plan:
         self.num_batches = info.num_batches
         self.num_rounds = info.num_rounds
         self.root = info.root
-        arrays = _lib.PlanArrays()
-        _check(lib.thmm_plan_get_arrays(self._handle, ctypes.byref(arrays)))
+        self._arrays = None
 
-        def grab(pointer, rows, width):
-            address = ctypes.cast(pointer, ctypes.c_void_p).value
-            return _view(address, rows * width, np.uint32).reshape(rows, width).copy()
+    _WIDTHS = {"edge_parents": ("num_edges", 1), "edge_children": ("num_edges", 1),
+               "rakes": ("num_branches", 4), "combinations": ("num_combinations", 3),
+               "absorptions": ("num_absorptions", 3),
+               "compressions": ("num_compressions", 6), "batches": ("num_batches", 3)}
 
-        self.edge_parents = grab(arrays.edge_parents, self.num_edges, 1).ravel()
-        self.edge_children = grab(arrays.edge_children, self.num_edges, 1).ravel()
-        self.rakes = grab(arrays.rakes, self.num_branches, 4)
-        self.combinations = grab(arrays.combinations, self.num_combinations, 3)
-        self.absorptions = grab(arrays.absorptions, self.num_absorptions, 3)
-        self.compressions = grab(arrays.compressions, self.num_compressions, 6)
-        self.batches = grab(arrays.batches, self.num_batches, 3)
+    def __getattr__(self, name):
+        # Operation arrays are copied out of the C++ plan on first use only.
+        if name not in Plan._WIDTHS:
+            raise AttributeError(name)
+        if self.__dict__.get("_arrays") is None:
+            arrays = _lib.PlanArrays()
+            _check(self._lib.thmm_plan_get_arrays(self._handle, ctypes.byref(arrays)))
+            self.__dict__["_arrays"] = arrays
+        rows_attr, width = Plan._WIDTHS[name]
+        rows = getattr(self, rows_attr)
+        address = ctypes.cast(getattr(self._arrays, name), ctypes.c_void_p).value
+        values = _view(address, rows * width, np.uint32).copy()
+        values = values if width == 1 else values.reshape(rows, width)
+        self.__dict__[name] = values
+        return values
 
     @property
     def handle(self) -> int:
