@@ -24,14 +24,32 @@ enum StepKind : std::uint32_t {
   kStepCombine = 1,
   kStepAbsorb = 2,
   kStepCompress = 3,
+  kStepGather = 4,
 };
 
-// Rake op (uint4):     path version, leaf (kFlag: value stored), branch, parent
+// Operation records (all indices are program-local):
+// Rake op (uint4):     path version, leaf (kFlag: value stored), parent,
+//                      observation slot of the leaf (kNone if unobserved).
+//                      The branch is implicit: rake i of the program fills
+//                      branch i (btrc numbers branches in rake order).
 // Combine op (uint2):  destination branch, source branch
-// Absorb op (uint2):   node (kFlag: first absorption, start from the input
-//                      factor), branch
-// Compress op (2 x uint4): {left version, middle (kFlag: stored), right
-//                      version, tape}, {parent, child, 0, 0}
+// Absorb op (uint4):   node (kFlag: first absorption, start from the input
+//                      factor), branch, observation slot of the node, 0
+// Compress op (uint4): left version, middle (kFlag: stored), right version,
+//                      observation slot of the middle node. The tape is
+//                      implicit: compression i of the program writes tape i.
+// Compress ends (uint2): parent, child (read only by MAP/sample expansion).
+// Gather op (uint4):   node (kFlag: first absorption), observation slot of
+//                      the node, first rake, rake count. Used only by the
+//                      sum-product forward: one round's rakes, branch
+//                      combinations and absorption into one parent fused into
+//                      a single operation (the rakes of a round are stored
+//                      grouped by parent so a gather's rakes are contiguous).
+//
+// A program has two step lists over the same operation arrays: the plan's
+// own primitive batches (MAP, sampling and the reverse sweep) and the fused
+// sum-product forward list (gather and compress steps).
+inline constexpr std::uint32_t kNone = 0xffffffffu;
 
 struct alignas(16) DevProgram {
   std::uint32_t step_begin;
@@ -40,15 +58,23 @@ struct alignas(16) DevProgram {
   std::uint32_t num_edges;
   std::uint32_t num_rakes;
   std::uint32_t num_compressions;
-  std::uint32_t root; // kFlag: the root has a stored (absorbed) value
-  std::uint32_t obs_map; // offset of this program's node -> observation map
+  std::uint32_t root;     // kFlag: the root has a stored (absorbed) value
+  std::uint32_t root_obs; // observation slot of the root, kNone if none
+  std::uint32_t rake_base;     // first rake op of the program
+  std::uint32_t compress_base; // first compress op of the program
+  std::uint32_t fused_begin;   // fused sum-product forward steps
+  std::uint32_t fused_count;
 };
 
 struct alignas(16) DevStep {
   std::uint32_t kind;
   std::uint32_t offset;
   std::uint32_t count;
-  std::uint32_t pad;
+  std::uint32_t aux_offset; // gather steps: the round's rakes
+  std::uint32_t aux_count;
+  std::uint32_t pad0;
+  std::uint32_t pad1;
+  std::uint32_t pad2;
 };
 
 // One tree instance: a program applied to one batch item (or one tree of a
@@ -80,8 +106,10 @@ struct EngineArgs {
   const DevStep *steps;
   const void *rakes;    // uint4
   const void *combines; // uint2
-  const void *absorbs;  // uint2
-  const void *compress; // 2 x uint4
+  const void *absorbs;  // uint4
+  const void *compress; // uint4
+  const void *compress_ends; // uint2
+  const void *gathers;       // uint4
   const DevInstance *instances;
   const std::uint32_t *big_items; // instances run by a whole CTA
   std::uint32_t big_count;
@@ -91,7 +119,6 @@ struct EngineArgs {
   std::uint32_t *error; // [1] ErrorBits
   const void *node_in;  // dense node factors
   const std::uint8_t *observations;
-  const std::int32_t *obs_map; // node -> observation slot, -1 if unobserved
   const void *root_potential;
   const void *emission;
   std::uint32_t categories;
@@ -122,10 +149,8 @@ inline ScratchSize InstanceScratch(std::uint64_t nodes, std::uint64_t rakes,
   const std::uint64_t matrix = states * states;
   ScratchSize size{};
   size.elements = nodes * states + rakes * states + compressions * matrix;
-  if (mode == kModeLinear && reverse) {
+  if (mode == kModeLinear && reverse)
     size.elements += compressions * matrix; // adjoints of compressed paths
-    size.bytes = compressions * 4;          // power-of-two exponents
-  }
   if (mode == kModeMaximum)
     size.bytes = rakes * states + compressions * matrix; // choice tapes
   size.bytes = (size.bytes + 15) & ~std::uint64_t{15};

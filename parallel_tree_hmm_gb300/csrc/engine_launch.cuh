@@ -13,9 +13,17 @@ namespace thmm {
 template <class Engine, typename Buffer, bool kGroupTiles>
 cudaError_t LaunchOrQuery(const EngineArgs &args, int grid, cudaStream_t stream,
                           int *blocks_per_sm) {
-  const std::size_t smem =
-      kGroupTiles ? std::size_t{kWarps} * 32 * Engine::G * sizeof(Buffer) : 0;
+  // Group tiles are only used when several lanes share an operation.
+  const std::size_t smem = kGroupTiles && Engine::G > 1
+                               ? std::size_t{kWarps} * 32 * Engine::G * sizeof(Buffer)
+                               : 0;
   auto kernel = EngineKernel<Engine, Buffer>;
+  if (smem > 48 * 1024) {
+    const cudaError_t status = cudaFuncSetAttribute(
+        kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
+    if (status != cudaSuccess)
+      return status;
+  }
   if (blocks_per_sm != nullptr)
     return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, kernel,
                                                          kThreads, smem);

@@ -29,12 +29,13 @@ struct ProgramSet {
   std::vector<DevStep> steps;
   std::vector<Uint4> rakes;
   std::vector<Uint2> combines;
-  std::vector<Uint2> absorbs;
-  std::vector<Uint4> compress; // two entries per operation
-  std::vector<std::int32_t> obs_map;
+  std::vector<Uint4> absorbs;
+  std::vector<Uint4> compress;
+  std::vector<Uint2> compress_ends;
+  std::vector<Uint4> gathers;
 
   // Appends the program of `plan`; `observation_nodes` (strictly increasing)
-  // builds the node -> observation-slot map when `categorical` is set.
+  // gives each observed node its observation slot (categorical models).
   std::uint32_t Add(const btrc::Plan &plan,
                     std::span<const std::uint32_t> observation_nodes,
                     bool categorical);

@@ -147,7 +147,7 @@ struct Workspace {
 
   // Device program.
   DeviceBuffer programs, steps, rakes, combines, absorbs, compress, instances;
-  DeviceBuffer big_items, small_items, obs_map, control;
+  DeviceBuffer compress_ends, gathers, big_items, small_items, control;
   std::uint32_t big_count = 0;
   std::uint32_t small_count = 0;
   bool items_big = false;
@@ -174,7 +174,7 @@ struct Workspace {
     }
     for (DeviceBuffer *buffer :
          {&programs, &steps, &rakes, &combines, &absorbs, &compress, &instances,
-          &big_items, &small_items, &obs_map, &control, &node_in, &edge_in,
+          &compress_ends, &gathers, &big_items, &small_items, &control, &node_in, &edge_in,
           &observations, &root_potential, &emission, &uniforms, &values,
           &node_out, &edge_out, &states_out, &scratch, &bytes})
       buffer->Free();
@@ -319,7 +319,8 @@ struct Workspace {
     combines.Upload(set.combines, stream);
     absorbs.Upload(set.absorbs, stream);
     compress.Upload(set.compress, stream);
-    obs_map.Upload(set.obs_map, stream);
+    compress_ends.Upload(set.compress_ends, stream);
+    gathers.Upload(set.gathers, stream);
     instances.Upload(table, stream);
     big_items.Upload(big, stream);
     small_items.Upload(small, stream);
@@ -496,6 +497,8 @@ struct Workspace {
     args.combines = combines.ptr;
     args.absorbs = absorbs.ptr;
     args.compress = compress.ptr;
+    args.compress_ends = compress_ends.ptr;
+    args.gathers = gathers.ptr;
     args.instances = instances.as<DevInstance>();
     args.big_items = big_items.as<std::uint32_t>();
     args.small_items = small_items.as<std::uint32_t>();
@@ -510,7 +513,6 @@ struct Workspace {
     args.error = control.as<std::uint32_t>() + 2;
     args.node_in = node_in.ptr;
     args.observations = observations.as<std::uint8_t>();
-    args.obs_map = obs_map.as<std::int32_t>();
     args.root_potential = root_potential.ptr;
     args.emission = emission.ptr;
     args.categories = static_cast<std::uint32_t>(categories);
