@@ -325,6 +325,36 @@ thmm_status thmm_workspace_synchronize(thmm_workspace *workspace);
 /* Kernel launches made by the most recent prepared call or enqueue. */
 uint64_t thmm_workspace_launches(const thmm_workspace *workspace);
 
+/* ---------------------------------------------------- allocation-free path */
+/* Size of the device array that holds every intermediate of
+ * thmm_log_partition_static. */
+#define THMM_STATIC_SCRATCH_BYTES (16u * 1024u * 1024u)
+
+/* No counterpart in the reference: an allocation-free variant of the batched
+ * log partition function (the scaled sum-product kernel behind
+ * thmm_log_partition_function), for callers that cannot call cudaMalloc, such
+ * as code whose device memory is owned by another allocator or code running
+ * where new allocations are not permitted. It makes no device, pinned or heap
+ * allocation on success: the compiled plan and all scratch of the contraction
+ * live in one static device array of THMM_STATIC_SCRATCH_BYTES that every GPU
+ * loading the library keeps until exit.
+ *
+ * Inputs and outputs are the caller's device buffers, FP32: node factors
+ * [batch, node, state], edge factors [edge, parent, child] shared by the batch,
+ * and log Z [batch]. Work is enqueued on `stream` (a cudaStream_t; NULL for
+ * the default stream) and the call returns without waiting for it.
+ *
+ * Limits and sharing: a plan and batch whose program and scratch exceed the
+ * static array are rejected with THMM_INVALID_ARGUMENT. The first call on a
+ * device resolves the array's device address (cudaGetSymbolAddress) and must
+ * come before any stream capture. Every call reuses the same array, which keeps
+ * the last call's contents; calls whose GPU work overlaps race, and the host
+ * side is not thread-safe. */
+thmm_status thmm_log_partition_static(const thmm_plan *plan, size_t states,
+                                      size_t batch, const float *node_potentials,
+                                      const float *edge_potentials,
+                                      float *log_partitions, void *stream);
+
 #ifdef __cplusplus
 }
 #endif

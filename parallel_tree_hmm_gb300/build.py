@@ -38,6 +38,7 @@ SOURCES = [
     "engine_linear_f64.cu",
     "engine_maximum.cu",
     "engine_sample.cu",
+    "static_scratch.cu",
 ]
 
 

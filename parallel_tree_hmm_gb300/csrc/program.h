@@ -13,15 +13,9 @@
 
 #include "btrc/plan.h"
 #include "engine.h"
+#include "program_builder.h"
 
 namespace thmm {
-
-struct Uint2 {
-  std::uint32_t x, y;
-};
-struct Uint4 {
-  std::uint32_t x, y, z, w;
-};
 
 // Programs of every distinct plan of a workspace, concatenated.
 struct ProgramSet {
@@ -33,6 +27,10 @@ struct ProgramSet {
   std::vector<Uint4> compress;
   std::vector<Uint2> compress_ends;
   std::vector<Uint4> gathers;
+
+  template <class T> std::vector<T> Temp(std::size_t count, T value) {
+    return std::vector<T>(count, value);
+  }
 
   // Appends the program of `plan`; `observation_nodes` (strictly increasing)
   // gives each observed node its observation slot (categorical models).

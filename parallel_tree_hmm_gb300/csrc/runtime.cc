@@ -779,6 +779,9 @@ constexpr const char *kReserveMarginalsMessage =
     "this plan, state count, and batch capacity";
 
 } // namespace
+
+void SetLastError(const char *message) { g_last_error = message; }
+
 } // namespace thmm
 
 using thmm::Guard;
