@@ -224,10 +224,11 @@ def main():
     local_rank = int(os.environ.get("LOCAL_RANK", "0"))
     dist = None
     if world > 1:
+        import torch
         import torch.distributed as dist  # noqa: F811
 
-        import torch
-        torch.cuda.set_device(local_rank)
+        if args.impl == "ours":
+            torch.cuda.set_device(local_rank)
         dist.init_process_group("nccl" if args.impl == "ours" else "gloo")
 
     if args.impl == "reference":
@@ -240,14 +241,21 @@ def main():
 
 
 def reduce_max(value, dist):
+    """Maximum of `value` over all ranks (the slowest rank's time)."""
     if dist is None:
         return value
     import torch
 
-    tensor = torch.tensor([value], dtype=torch.float64,
-                          device="cuda" if torch.cuda.is_available() else "cpu")
+    on_gpu = dist.get_backend() == "nccl"
+    tensor = torch.tensor([value], dtype=torch.float64, device="cuda" if on_gpu else "cpu")
     dist.all_reduce(tensor, op=dist.ReduceOp.MAX)
     return float(tensor.item())
+
+
+def rank_seed(seed: int, rank: int) -> int:
+    """Each rank contracts its own forest replica (weak scaling, no
+    collective on the data path); replicas differ only by seed."""
+    return seed + 1000 * rank
 
 
 def run_reference(args, rank, world, dist):
@@ -295,10 +303,10 @@ def run_ours(args, rank, world, local_rank, dist):
 
     device = local_rank
     torch.cuda.set_device(device)
-    forest = Forest(args.trees, args.states, args.seed + 1000 * rank)
+    forest = Forest(args.trees, args.states, rank_seed(args.seed, rank))
     K = forest.states
     plans = [thmm.Plan(p) for p in forest.parents]
-    factor_sets = [forest.factors(args.seed + 1 + i + 1000 * rank) for i in range(2)]
+    factor_sets = [forest.factors(rank_seed(args.seed, rank) + 1 + i) for i in range(2)]
     observations = forest.observations()
 
     def reserve(compute):
