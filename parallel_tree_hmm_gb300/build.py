@@ -82,6 +82,32 @@ def build_library(jobs: int | None = None) -> pathlib.Path:
     return LIBRARY
 
 
+def build_cpp_tests() -> list[pathlib.Path]:
+    """Compiles tests/cpp/accelerator_dropin_test.cc (C++ API drop-in check)
+    in the FP64 and FP32 precisions against the in-tree library and the
+    oracle; the GPU tests run the binaries."""
+    source = ROOT / "tests" / "cpp" / "accelerator_dropin_test.cc"
+    outputs = []
+    for tag, defines in (("f64", []), ("f32", ["-DTREE_HMM_USE_FLOAT=1"])):
+        binary = source.with_name(f"accelerator_dropin_test_{tag}")
+        inputs = [source, LIBRARY, ROOT / "oracle" / "liboracle.so",
+                  *(ROOT / "include").rglob("*.h")]
+        if binary.exists() and binary.stat().st_mtime >= max(p.stat().st_mtime for p in inputs):
+            outputs.append(binary)
+            continue
+        cuda_include = pathlib.Path(nvcc()).resolve().parent.parent / "include"
+        cmd = [os.environ.get("CXX", "g++"), "-std=c++20", "-O2", *defines,
+               f"-I{ROOT / 'include'}", f"-I{ROOT / 'oracle'}", f"-I{cuda_include}",
+               str(source), "-o", str(binary), f"-L{PACKAGE}", "-lthmm_gb300",
+               f"-L{ROOT / 'oracle'}", "-loracle", f"-Wl,-rpath,{PACKAGE}",
+               f"-Wl,-rpath,{ROOT / 'oracle'}"]
+        result = subprocess.run(cmd, capture_output=True, text=True)
+        if result.returncode != 0:
+            raise RuntimeError(f"C++ test build failed:\n{result.stderr}")
+        outputs.append(binary)
+    return outputs
+
+
 def build_oracle(reference: bool = True) -> None:
     """Builds the C oracle (test infrastructure) and, when the reference tree
     is present, the reference CPU library and tests under oracle/_ref."""
@@ -95,3 +121,4 @@ def build_oracle(reference: bool = True) -> None:
 if __name__ == "__main__":
     print(build_library())
     build_oracle()
+    print(build_cpp_tests())
