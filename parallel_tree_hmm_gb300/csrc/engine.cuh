@@ -1,9 +1,9 @@
 // Persistent tree-contraction kernels for sm_103a.
 //
 // Work decomposition. A *team* contracts one tree instance at a time: a whole
-// CTA (256 threads) for large trees, a single warp for small ones. Instances
+// CTA (128 threads) for large trees, a single warp for small ones. Instances
 // come from two queues (largest first) through one atomic counter each; a CTA
-// drains the large-tree queue first and then splits into eight warp teams for
+// drains the large-tree queue first and then splits into four warp teams for
 // the small trees. Inside a team the plan's steps run in order with a team
 // barrier in between (the operations of one step are independent, as in a
 // btrc::PrimitiveBatch). Each operation of a step is handled by a *group* of
@@ -39,7 +39,15 @@
 
 namespace thmm {
 
-constexpr int kThreads = 256;
+// 128-thread CTAs, four per SM: measured fastest on the uneven K=4 forest
+// against 64/256/512 threads and higher forced occupancy (which spills).
+#ifndef THMM_CTA_THREADS
+#define THMM_CTA_THREADS 128
+#endif
+#ifndef THMM_MIN_CTAS_PER_SM
+#define THMM_MIN_CTAS_PER_SM 4
+#endif
+constexpr int kThreads = THMM_CTA_THREADS;
 constexpr int kWarps = kThreads / 32;
 constexpr unsigned kFull = 0xffffffffu;
 
@@ -1335,7 +1343,8 @@ template <typename T, int KMAX> struct SampleEngine {
 
 // --------------------------------------------------------------- kernel --
 template <class Engine, typename Buffer>
-__global__ void __launch_bounds__(kThreads) EngineKernel(EngineArgs args) {
+__global__ void __launch_bounds__(kThreads, THMM_MIN_CTAS_PER_SM)
+EngineKernel(EngineArgs args) {
   extern __shared__ __align__(16) unsigned char dynamic_smem[];
   __shared__ SharedState shared;
   Buffer *buffers = reinterpret_cast<Buffer *>(dynamic_smem);

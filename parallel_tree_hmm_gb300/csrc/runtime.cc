@@ -105,10 +105,11 @@ struct HostBuffer {
   ~HostBuffer() { Free(); }
 };
 
+// Trees with at least this many nodes get a whole CTA; smaller ones a warp.
 int TeamThreshold() {
   if (const char *value = std::getenv("THMM_TEAM_THRESHOLD"))
     return std::max(1, std::atoi(value));
-  return 2048;
+  return 1024;
 }
 
 } // namespace

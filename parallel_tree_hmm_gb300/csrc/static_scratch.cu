@@ -152,7 +152,7 @@ DeviceSetup &Setup(int device) {
 int TeamThresholdStatic() {
   if (const char *value = std::getenv("THMM_TEAM_THRESHOLD"))
     return std::max(1, std::atoi(value));
-  return 2048;
+  return 1024;
 }
 
 } // namespace
