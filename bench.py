@@ -52,14 +52,14 @@ UNIT = "nodes/s"
 def parse_args():
     parser = argparse.ArgumentParser()
     parser.add_argument("--gpus", type=int, default=1)
-    parser.add_argument("--steps", type=int, default=20)
+    parser.add_argument("--steps", type=int, default=100)
     parser.add_argument("--warmup", type=int, default=3)
     parser.add_argument("--impl", choices=["ours", "reference"], default="ours")
     parser.add_argument("--states", type=int, default=4)
     parser.add_argument("--trees", type=int, default=4096)
     parser.add_argument("--seed", type=int, default=0)
     parser.add_argument("--e2e-steps", type=int, default=None)
-    parser.add_argument("--cpu-sample-nodes", type=int, default=8_000_000)
+    parser.add_argument("--cpu-sample-nodes", type=int, default=20_000_000)
     return parser.parse_args()
 
 
@@ -129,7 +129,7 @@ class ClockSampler:
         try:
             self.process = subprocess.Popen(
                 ["nvidia-smi", f"--id={self.device}", f"--query-gpu={self.FIELDS}",
-                 "--format=csv,noheader,nounits", "-lms", "200"],
+                 "--format=csv,noheader,nounits", "-lms", "50"],
                 stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             self.thread = threading.Thread(target=self._read, daemon=True)
             self.thread.start()
@@ -382,7 +382,7 @@ def run_ours(args, rank, world, local_rank, dist):
         stage(ws, factor_sets[i % 2])
         ws.posterior_marginals_prepared(staged, thmm.CategoricalInputUpdate.kFactors)
     e2e_total = 0.0
-    api_kernel_ms = []
+    api_kernel_ms, api_upload_ms, api_download_ms = [], [], []
     for i in range(e2e_steps):
         stage(ws, factor_sets[i % 2])
         torch.cuda.synchronize(device)
@@ -392,6 +392,8 @@ def run_ours(args, rank, world, local_rank, dist):
         result = ws.posterior_marginals_prepared(staged, thmm.CategoricalInputUpdate.kFactors)
         e2e_total += time.perf_counter() - begin
         api_kernel_ms.append(result.timings.kernel_ms)
+        api_upload_ms.append(result.timings.upload_ms)
+        api_download_ms.append(result.timings.download_ms)
     e2e_total = reduce_max(e2e_total, dist)
     e2e_value = forest.total_nodes * world * e2e_steps / e2e_total
     S = 4
@@ -428,7 +430,9 @@ def run_ours(args, rank, world, local_rank, dist):
                      "algorithmic_bytes_per_launch": algorithmic},
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d,
                 "d2h_bytes_per_step": d2h,
-                "api_kernel_ms_median": statistics.median(api_kernel_ms)},
+                "api_kernel_ms_median": statistics.median(api_kernel_ms),
+                "api_upload_ms_median": statistics.median(api_upload_ms),
+                "api_download_ms_median": statistics.median(api_download_ms)},
         "gpu_launches": args.steps,
         "clocks": sampler.summary(),
     }
