@@ -333,7 +333,7 @@ def run_ours(args, rank, world, local_rank, dist):
     node_sum = first.nodes.reshape(-1, K).sum(axis=1)
     normalisation_error = float(np.max(np.abs(node_sum - 1.0)))
 
-    stream = torch.cuda.ExternalStream(ws.stream, device=device)
+    tuning = ws.autotune(4, repeats=3)
 
     def device_time(workspace, steps, warmup, sampler=None):
         ext = torch.cuda.ExternalStream(workspace.stream, device=device)
@@ -359,6 +359,7 @@ def run_ours(args, rank, world, local_rank, dist):
     sampler = ClockSampler(device)
     with sampler:
         elapsed_ms, nodes_done = device_time(ws, args.steps, args.warmup)
+    launches_per_step = ws.launches
     elapsed_ms = reduce_max(elapsed_ms, dist)
     launch_ms = elapsed_ms / args.steps
     value = nodes_done * world / (elapsed_ms / 1e3)
@@ -368,6 +369,7 @@ def run_ours(args, rank, world, local_rank, dist):
     staged64 = stage(ws64, factor_sets[0])
     staged64.observations[:] = observations
     plain = ws64.posterior_marginals_prepared(staged64, thmm.CategoricalInputUpdate.kAll)
+    plain_tuning = ws64.autotune(4, repeats=2)
     plain_logz_diff = float(np.max(np.abs(plain.log_partitions.astype(np.float64)
                                           - log_z_reference.astype(np.float64))
                                    / np.maximum(1.0, np.abs(plain.log_partitions))))
@@ -382,7 +384,8 @@ def run_ours(args, rank, world, local_rank, dist):
         stage(ws, factor_sets[i % 2])
         ws.posterior_marginals_prepared(staged, thmm.CategoricalInputUpdate.kFactors)
     e2e_total = 0.0
-    api_kernel_ms, api_upload_ms, api_download_ms = [], [], []
+    api_kernel_ms, api_upload_ms, api_download_ms, api_wall_ms = [], [], [], []
+    call_ms = []
     for i in range(e2e_steps):
         stage(ws, factor_sets[i % 2])
         torch.cuda.synchronize(device)
@@ -390,10 +393,12 @@ def run_ours(args, rank, world, local_rank, dist):
             dist.barrier()
         begin = time.perf_counter()
         result = ws.posterior_marginals_prepared(staged, thmm.CategoricalInputUpdate.kFactors)
-        e2e_total += time.perf_counter() - begin
+        call_ms.append(1e3 * (time.perf_counter() - begin))
+        e2e_total += call_ms[-1] / 1e3
         api_kernel_ms.append(result.timings.kernel_ms)
         api_upload_ms.append(result.timings.upload_ms)
         api_download_ms.append(result.timings.download_ms)
+        api_wall_ms.append(result.timings.wall_ms)
     e2e_total = reduce_max(e2e_total, dist)
     e2e_value = forest.total_nodes * world * e2e_steps / e2e_total
     S = 4
@@ -422,6 +427,7 @@ def run_ours(args, rank, world, local_rank, dist):
                    "plain_fp64_nodes_per_s": plain_value,
                    "chosen_over_plain_fp64": value / plain_value,
                    "plain_fp64_log_z_rel_diff": plain_logz_diff,
+                   "tuning": tuning, "plain_fp64_tuning": plain_tuning,
                    "node_marginal_normalisation_error": normalisation_error},
         "roofline": {"bound": "hbm", "achieved": achieved,
                      "peak": peak, "unit": "GB/s", "frac": achieved / peak,
@@ -432,8 +438,13 @@ def run_ours(args, rank, world, local_rank, dist):
                 "d2h_bytes_per_step": d2h,
                 "api_kernel_ms_median": statistics.median(api_kernel_ms),
                 "api_upload_ms_median": statistics.median(api_upload_ms),
-                "api_download_ms_median": statistics.median(api_download_ms)},
-        "gpu_launches": args.steps,
+                "api_download_ms_median": statistics.median(api_download_ms),
+                "api_wall_ms_median": statistics.median(api_wall_ms),
+                "call_ms_median": statistics.median(call_ms),
+                "call_ms": [round(v, 3) for v in call_ms],
+                "api_wall_ms": [round(v, 3) for v in api_wall_ms],
+                "stripes": ws.launches // 2},
+        "gpu_launches": args.steps * launches_per_step,
         "clocks": sampler.summary(),
     }
     if rank == 0 and world == 1 and args.cpu_sample_nodes > 0:

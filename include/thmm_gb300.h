@@ -148,8 +148,8 @@ thmm_status thmm_reserve_categorical(thmm_workspace *workspace,
 
 /* Extension (no reference counterpart: the reference batch shares one
  * topology, include/tree_hmm/accelerator.h:13-23). A forest of `tree_count`
- * independent trees, each with its own plan and its own edge factors, run in
- * one launch. Node and edge arrays are the per-tree arrays concatenated in
+ * independent trees, each with its own plan and its own edge factors, run by
+ * the same persistent launches. Node and edge arrays are the per-tree arrays concatenated in
  * tree order. */
 thmm_status thmm_reserve_forest(thmm_workspace *workspace,
                                 const thmm_plan *const *plans,
@@ -311,13 +311,40 @@ thmm_status thmm_categorical_posterior_marginals(
     thmm_workspace *workspace, const thmm_categorical_model *model,
     int update, thmm_marginal_result *out);
 
-/* Extension for device-resident timing and CUDA-graph capture (no reference
- * counterpart). Enqueues only the device work of `operation` on the
- * workspace stream, reading the inputs left resident by the previous prepared
- * call of the same workspace; no host copies and no synchronisation.
- * `nodes_out` (optional) receives the number of tree nodes processed. */
+/* Extension for device-resident timing (no reference counterpart). Enqueues
+ * only the device work of `operation` on the workspace stream, reading the
+ * inputs left resident by the previous prepared call of the same workspace;
+ * no host copies and no synchronisation. The step (work-counter memset and
+ * kernel launches) is captured into a CUDA graph on its first use per
+ * operation and batch and replayed afterwards; a new tuning or reservation
+ * drops the graphs. `nodes_out` (optional) receives the number of tree nodes
+ * processed. */
 thmm_status thmm_enqueue(thmm_workspace *workspace, int operation,
                          uint64_t *nodes_out);
+
+/* Launch tuning of a workspace (extension, no reference counterpart). Trees
+ * with at least `team_threshold` nodes are contracted by a whole CTA, smaller
+ * ones by a single warp. `ctas_per_sm[k]` caps the resident CTAs per SM of
+ * kernel k (0: forward sum-product sweep, 1: MAP, 2: sampling, 3: adjoint
+ * sweep of the marginals); 0 means the occupancy limit. A prepared call is
+ * cut into `stripes` (1 to 8; 0: one per 2 Mi nodes) contiguous runs of
+ * instances whose input copies, kernels and output copies overlap. No
+ * setting changes any result bit. */
+typedef struct thmm_tuning {
+  uint32_t team_threshold;
+  uint32_t ctas_per_sm[4];
+  uint32_t stripes;
+  float kernel_ms;     /* device time per step of the chosen setting */
+  uint32_t candidates; /* settings timed by the last autotune */
+} thmm_tuning;
+/* Times candidate settings for `operation` on the inputs left resident by a
+ * prepared call (`repeats` timed steps each, after one untimed step), keeps
+ * the fastest and returns it. Overwrites the workspace outputs with the same
+ * values. */
+thmm_status thmm_autotune(thmm_workspace *workspace, int operation, int repeats,
+                          thmm_tuning *out);
+thmm_status thmm_get_tuning(const thmm_workspace *workspace, thmm_tuning *out);
+thmm_status thmm_set_tuning(thmm_workspace *workspace, const thmm_tuning *tuning);
 /* The workspace's cudaStream_t, as an opaque pointer. */
 void *thmm_workspace_stream(thmm_workspace *workspace);
 thmm_status thmm_workspace_synchronize(thmm_workspace *workspace);

@@ -110,6 +110,11 @@ class MarginalResult(ctypes.Structure):
                 ("timings", Timings)]
 
 
+class Tuning(ctypes.Structure):
+    _fields_ = [("team_threshold", c_u32), ("ctas_per_sm", c_u32 * 4),
+                ("stripes", c_u32), ("kernel_ms", ctypes.c_float), ("candidates", c_u32)]
+
+
 # name -> (restype, argtypes)
 PROTOTYPES = {
     "thmm_last_error": (ctypes.c_char_p, []),
@@ -161,6 +166,9 @@ PROTOTYPES = {
         c_int, [c_void_p, ctypes.POINTER(CategoricalModel), c_int,
                 ctypes.POINTER(MarginalResult)]),
     "thmm_enqueue": (c_int, [c_void_p, c_int, ctypes.POINTER(c_u64)]),
+    "thmm_autotune": (c_int, [c_void_p, c_int, c_int, ctypes.POINTER(Tuning)]),
+    "thmm_get_tuning": (c_int, [c_void_p, ctypes.POINTER(Tuning)]),
+    "thmm_set_tuning": (c_int, [c_void_p, ctypes.POINTER(Tuning)]),
     "thmm_workspace_stream": (c_void_p, [c_void_p]),
     "thmm_workspace_synchronize": (c_int, [c_void_p]),
     "thmm_workspace_launches": (c_u64, [c_void_p]),

@@ -232,9 +232,12 @@ class Workspace:
 
     @staticmethod
     def _flags(kind: str, compute) -> int:
-        flags = {"": 0, "maximum": _lib.THMM_RESERVE_MAXIMUM,
+        table = {"": 0, "maximum": _lib.THMM_RESERVE_MAXIMUM,
                  "sampling": _lib.THMM_RESERVE_SAMPLING,
-                 "marginals": _lib.THMM_RESERVE_MARGINALS}[kind]
+                 "marginals": _lib.THMM_RESERVE_MARGINALS}
+        flags = 0
+        for part in kind.split(","):  # e.g. "maximum,sampling"
+            flags |= table[part.strip()]
         if compute is not None and np.dtype(compute) == np.float64:
             flags |= _lib.THMM_COMPUTE_F64
         return flags
@@ -476,6 +479,29 @@ class Workspace:
         _check(self._lib.thmm_enqueue(self._handle, operation, ctypes.byref(nodes)))
         return nodes.value
 
+    def autotune(self, operation: int = 4, repeats: int = 3) -> dict:
+        """Times candidate team thresholds and CTAs per SM for `operation`
+        (thmm_enqueue codes) on the resident inputs and keeps the fastest."""
+        tuning = _lib.Tuning()
+        _check(self._lib.thmm_autotune(self._handle, operation, repeats,
+                                       ctypes.byref(tuning)))
+        return _tuning_dict(tuning)
+
+    @property
+    def tuning(self) -> dict:
+        tuning = _lib.Tuning()
+        _check(self._lib.thmm_get_tuning(self._handle, ctypes.byref(tuning)))
+        return _tuning_dict(tuning)
+
+    def set_tuning(self, team_threshold: int, ctas_per_sm=(0, 0, 0, 0),
+                   stripes: int = 0) -> None:
+        tuning = _lib.Tuning()
+        tuning.team_threshold = team_threshold
+        for i, value in enumerate(ctas_per_sm):
+            tuning.ctas_per_sm[i] = value
+        tuning.stripes = stripes
+        _check(self._lib.thmm_set_tuning(self._handle, ctypes.byref(tuning)))
+
     @property
     def stream(self) -> int:
         return self._lib.thmm_workspace_stream(self._handle)
@@ -486,6 +512,13 @@ class Workspace:
     @property
     def launches(self) -> int:
         return self._lib.thmm_workspace_launches(self._handle)
+
+
+def _tuning_dict(tuning) -> dict:
+    return {"team_threshold": int(tuning.team_threshold),
+            "ctas_per_sm": [int(v) for v in tuning.ctas_per_sm],
+            "stripes": int(tuning.stripes),
+            "kernel_ms": float(tuning.kernel_ms), "candidates": int(tuning.candidates)}
 
 
 def available() -> bool:

@@ -39,13 +39,16 @@
 
 namespace thmm {
 
-// 128-thread CTAs, four per SM: measured fastest on the uneven K=4 forest
-// against 64/256/512 threads and higher forced occupancy (which spills).
+// 128-thread CTAs: measured fastest on the uneven K=4 forest against
+// 64/256/512 threads.
 #ifndef THMM_CTA_THREADS
 #define THMM_CTA_THREADS 128
 #endif
-#ifndef THMM_MIN_CTAS_PER_SM
-#define THMM_MIN_CTAS_PER_SM 4
+#ifndef THMM_FORWARD_MIN_CTAS_K4
+#define THMM_FORWARD_MIN_CTAS_K4 6
+#endif
+#ifndef THMM_REVERSE_MIN_CTAS_K4
+#define THMM_REVERSE_MIN_CTAS_K4 5
 #endif
 constexpr int kThreads = THMM_CTA_THREADS;
 constexpr int kWarps = kThreads / 32;
@@ -383,7 +386,28 @@ template <typename Scalar, typename Compute, int KMAX> struct Context {
 };
 
 // ------------------------------------------------------- sum-product --
-template <typename Scalar, typename Compute, int KMAX> struct LinearEngine {
+// The sum-product forward sweep (log Z, and the root marginal when marginals
+// are wanted) and the adjoint sweep are separate launches: each gets its own
+// register allocation, so the smaller forward runs at a higher occupancy.
+enum LinearPart : int { kLinearForward = 0, kLinearReverse = 1 };
+
+// Minimum resident CTAs per SM requested from the compiler for each part,
+// padded state count and arithmetic width (a register cap of
+// 65536 / (128 * n) per thread), chosen so that no variant spills much.
+template <int KMAX, int kPart, bool kWide> constexpr int LinearMinBlocks() {
+  if constexpr (KMAX <= 4 && !kWide)
+    return kPart == kLinearForward ? THMM_FORWARD_MIN_CTAS_K4 : THMM_REVERSE_MIN_CTAS_K4;
+  else if constexpr (KMAX <= 4)
+    return kPart == kLinearForward ? 4 : 2;
+  else if constexpr (KMAX <= 8 || (KMAX <= 16 && !kWide))
+    return 4;
+  else
+    return 2;
+}
+
+template <typename Scalar, typename Compute, int KMAX, int kPart = kLinearForward>
+struct LinearEngine {
+  static constexpr int kMinBlocks = LinearMinBlocks<KMAX, kPart, sizeof(Compute) == 8>();
   static constexpr int G = GroupLanes<KMAX>();
   static constexpr int ROWS = KMAX / G;
   using Ctx = Context<Scalar, Compute, KMAX>;
@@ -738,39 +762,38 @@ template <typename Scalar, typename Compute, int KMAX> struct LinearEngine {
               ratio[q][j] = ratio[q][j] > Compute(0) ? adjoint[j] / ratio[q][j]
                                                      : Compute(0);
           }
-          // Left adjoint rows: left[r][m] middle[m] sum_j right[m][j] ratio[r][j].
-          Compute left_adjoint[ROWS][KMAX];
+          // Left adjoint rows: left[r][m] middle[m] sum_j right[m][j] ratio[r][j],
+          // one row at a time (stored as soon as it is complete).
           Compute rights[G == 1 ? KMAX : 1][KMAX];
+          if constexpr (G == 1) {
 #pragma unroll
-          for (int q = 0; q < ROWS; ++q)
+            for (unsigned mid = 0; mid < KMAX; ++mid)
+              PathRow(op.z, mid, rights[mid]);
+          }
 #pragma unroll
-            for (unsigned j = 0; j < KMAX; ++j)
-              left_adjoint[q][j] = Compute(0);
+          for (int q = 0; q < ROWS; ++q) {
+            Compute left_adjoint[KMAX];
 #pragma unroll
-          for (unsigned mid = 0; mid < KMAX; ++mid) {
-            if (mid < K) {
-              Compute right[KMAX];
-              PathRow(op.z, mid, right);
-              if constexpr (G == 1) {
+            for (unsigned mid = 0; mid < KMAX; ++mid) {
+              left_adjoint[mid] = Compute(0);
+              if (mid < K) {
+                Compute right[KMAX];
+                if constexpr (G == 1) {
 #pragma unroll
-                for (unsigned j = 0; j < KMAX; ++j)
-                  rights[mid][j] = right[j];
-              }
-#pragma unroll
-              for (int q = 0; q < ROWS; ++q) {
+                  for (unsigned j = 0; j < KMAX; ++j)
+                    right[j] = rights[mid][j];
+                } else {
+                  PathRow(op.z, mid, right);
+                }
                 Compute dot = Compute(0);
 #pragma unroll
                 for (unsigned j = 0; j < KMAX; ++j)
                   dot = fma(right[j], ratio[q][j], dot);
-                left_adjoint[q][mid] = left[q][mid] * middle[mid] * dot;
+                left_adjoint[mid] = left[q][mid] * middle[mid] * dot;
               }
             }
-          }
-          if (active) {
-#pragma unroll
-            for (int q = 0; q < ROWS; ++q)
-              if (lane + q * G < K)
-                StorePathAdjoint(op.x, lane + q * G, left_adjoint[q], edge_out);
+            if (active && lane + q * G < K)
+              StorePathAdjoint(op.x, lane + q * G, left_adjoint, edge_out);
           }
           // Right adjoint rows m: right[m][j] middle[m] sum_p left[p][m] ratio[p][j].
           if constexpr (G == 1) {
@@ -845,6 +868,10 @@ template <typename Scalar, typename Compute, int KMAX> struct LinearEngine {
 
   template <bool kCta>
   __device__ void Run(const Team<kCta> &team, unsigned item, SharedState &sh) {
+    if constexpr (kPart == kLinearReverse) {
+      Reverse(team);
+      return;
+    }
     Forward(team);
     long long total = exponent;
     int flag = zero;
@@ -875,10 +902,6 @@ template <typename Scalar, typename Compute, int KMAX> struct LinearEngine {
           root_out[j] = static_cast<Scalar>(finite ? value / sum : 0.0);
         }
       }
-    }
-    if (c.a.reverse) {
-      team.sync();
-      Reverse(team);
     }
   }
 };
@@ -920,6 +943,7 @@ template <typename T, int KMAX> struct LogContext {
 
 // -------------------------------------------------------- max-product --
 template <typename T, int KMAX> struct MaxEngine {
+  static constexpr int kMinBlocks = KMAX <= 8 ? 4 : 2;
   static constexpr int G = GroupLanes<KMAX>();
   static constexpr int ROWS = KMAX / G;
   LogContext<T, KMAX> lc;
@@ -1162,6 +1186,7 @@ __device__ __forceinline__ unsigned SampleLogWeights(const T (&terms)[KMAX],
 }
 
 template <typename T, int KMAX> struct SampleEngine {
+  static constexpr int kMinBlocks = KMAX <= 8 ? 4 : 2;
   static constexpr int G = GroupLanes<KMAX>();
   static constexpr int ROWS = KMAX / G;
   LogContext<T, KMAX> lc;
@@ -1343,7 +1368,7 @@ template <typename T, int KMAX> struct SampleEngine {
 
 // --------------------------------------------------------------- kernel --
 template <class Engine, typename Buffer>
-__global__ void __launch_bounds__(kThreads, THMM_MIN_CTAS_PER_SM)
+__global__ void __launch_bounds__(kThreads, Engine::kMinBlocks)
 EngineKernel(EngineArgs args) {
   extern __shared__ __align__(16) unsigned char dynamic_smem[];
   __shared__ SharedState shared;

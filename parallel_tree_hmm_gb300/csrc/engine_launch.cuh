@@ -31,25 +31,37 @@ cudaError_t LaunchOrQuery(const EngineArgs &args, int grid, cudaStream_t stream,
   return cudaGetLastError();
 }
 
-template <typename Scalar, typename Compute>
-cudaError_t LaunchLinearTyped(unsigned kmax, const EngineArgs &args, int grid,
-                              cudaStream_t stream, int *blocks_per_sm) {
+template <typename Scalar, typename Compute, int kPart>
+cudaError_t LaunchLinearPart(unsigned kmax, const EngineArgs &args, int grid,
+                             cudaStream_t stream, int *blocks_per_sm) {
   switch (kmax) {
   case 4:
-    return LaunchOrQuery<LinearEngine<Scalar, Compute, 4>, Compute, true>(
+    return LaunchOrQuery<LinearEngine<Scalar, Compute, 4, kPart>, Compute, true>(
         args, grid, stream, blocks_per_sm);
   case 8:
-    return LaunchOrQuery<LinearEngine<Scalar, Compute, 8>, Compute, true>(
+    return LaunchOrQuery<LinearEngine<Scalar, Compute, 8, kPart>, Compute, true>(
         args, grid, stream, blocks_per_sm);
   case 16:
-    return LaunchOrQuery<LinearEngine<Scalar, Compute, 16>, Compute, true>(
+    return LaunchOrQuery<LinearEngine<Scalar, Compute, 16, kPart>, Compute, true>(
         args, grid, stream, blocks_per_sm);
   case 32:
-    return LaunchOrQuery<LinearEngine<Scalar, Compute, 32>, Compute, true>(
+    return LaunchOrQuery<LinearEngine<Scalar, Compute, 32, kPart>, Compute, true>(
         args, grid, stream, blocks_per_sm);
   default:
     return cudaErrorInvalidValue;
   }
+}
+
+// `part` selects the forward sweep (kLinearForward) or the adjoint sweep
+// (kLinearReverse).
+template <typename Scalar, typename Compute>
+cudaError_t LaunchLinearTyped(unsigned kmax, int part, const EngineArgs &args, int grid,
+                              cudaStream_t stream, int *blocks_per_sm) {
+  return part == kLinearReverse
+             ? LaunchLinearPart<Scalar, Compute, kLinearReverse>(kmax, args, grid, stream,
+                                                                 blocks_per_sm)
+             : LaunchLinearPart<Scalar, Compute, kLinearForward>(kmax, args, grid, stream,
+                                                                 blocks_per_sm);
 }
 
 template <template <typename, int> class Engine, typename T>

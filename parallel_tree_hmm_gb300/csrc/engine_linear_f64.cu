@@ -3,12 +3,12 @@
 
 namespace thmm {
 
-cudaError_t LaunchLinearF64(bool compute_f64, unsigned kmax,
+cudaError_t LaunchLinearF64(bool compute_f64, unsigned kmax, int part,
                             const EngineArgs &args, int grid,
                             cudaStream_t stream, int *blocks_per_sm) {
-  return compute_f64 ? LaunchLinearTyped<double, double>(kmax, args, grid,
+  return compute_f64 ? LaunchLinearTyped<double, double>(kmax, part, args, grid,
                                                          stream, blocks_per_sm)
-                     : LaunchLinearTyped<double, float>(kmax, args, grid,
+                     : LaunchLinearTyped<double, float>(kmax, part, args, grid,
                                                         stream, blocks_per_sm);
 }
 

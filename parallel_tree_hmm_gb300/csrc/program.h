@@ -40,11 +40,13 @@ struct ProgramSet {
 };
 
 // Kernel entry points. `kmax` is the padded state count (4, 8, 16 or 32).
-// With `blocks_per_sm` non-null the call only reports the occupancy.
-cudaError_t LaunchLinearF32(bool compute_f64, unsigned kmax,
+// With `blocks_per_sm` non-null the call only reports the occupancy. The
+// linear (sum-product) kernels come in two parts: 0 = forward sweep (log Z,
+// root marginal), 1 = adjoint sweep (marginals), launched in that order.
+cudaError_t LaunchLinearF32(bool compute_f64, unsigned kmax, int part,
                             const EngineArgs &args, int grid,
                             cudaStream_t stream, int *blocks_per_sm);
-cudaError_t LaunchLinearF64(bool compute_f64, unsigned kmax,
+cudaError_t LaunchLinearF64(bool compute_f64, unsigned kmax, int part,
                             const EngineArgs &args, int grid,
                             cudaStream_t stream, int *blocks_per_sm);
 cudaError_t LaunchMaximum(int scalar_bytes, unsigned kmax,

@@ -8,7 +8,8 @@
 // events for the upload/kernel/download split plus a wall clock, and the same
 // exception classes (reported here as status codes). Where the reference
 // launches one kernel per primitive batch and phase, a prepared call here
-// launches one persistent kernel (engine.cuh) after a small memset.
+// launches one persistent kernel (engine.cuh) after a small memset, two for
+// marginals (forward sweep, then adjoint sweep).
 #include "thmm_gb300.h"
 
 #include <algorithm>
@@ -22,7 +23,9 @@
 #include <numeric>
 #include <stdexcept>
 #include <string>
+#include <tuple>
 #include <unordered_map>
+#include <utility>
 #include <vector>
 
 #include <cuda_runtime.h>
@@ -148,10 +151,55 @@ struct Workspace {
 
   // Device program.
   DeviceBuffer programs, steps, rakes, combines, absorbs, compress, instances;
-  DeviceBuffer compress_ends, gathers, big_items, small_items, control;
+  DeviceBuffer compress_ends, gathers, team_order, control;
   std::uint32_t big_count = 0;
   std::uint32_t small_count = 0;
   bool items_big = false;
+
+  // Team assignment and grid. `team_order` lists the instances largest
+  // first; the first `big_count` (instances with at least `team_threshold`
+  // nodes) are contracted by whole CTAs, the rest by single warps.
+  // `cta_cap[slot]` (0 = none) caps the resident CTAs per SM of one kernel
+  // below its occupancy limit. Both are tunable (Autotune) and leave every
+  // result bit-identical.
+  std::vector<std::uint64_t> sorted_nodes;
+  std::uint32_t team_threshold = 0;
+  int cta_cap[4] = {0, 0, 0, 0};
+  float tuned_ms = 0.0f;
+
+  // Instantiated CUDA graphs of the device-only step, per operation and batch.
+  struct Graph {
+    int operation;
+    std::size_t batch;
+    cudaGraphExec_t exec;
+  };
+  std::vector<Graph> graphs;
+
+  // Striped prepared calls. The instances of a call are cut into up to
+  // kMaxStripes contiguous stripes of about equal node count; stripe c's
+  // inputs are copied on `copy_in`, its kernels run on `stream` once they
+  // have arrived, and its outputs are copied back on `copy_out` while later
+  // stripes still compute, so the host<->device copies of one call overlap
+  // each other and the kernels. `stripe_order` holds each stripe's instances
+  // largest first at the stripe's own position.
+  static constexpr std::uint32_t kMaxStripes = 8;
+  static constexpr std::uint64_t kNodesPerStripe = 2u << 20;
+  struct Stripe {
+    std::uint32_t first, last; // instance range
+    std::uint32_t big, small;  // CTA and warp team counts
+  };
+  std::vector<Stripe> stripe_plan;
+  std::size_t stripe_batch = 0;
+  std::uint32_t stripe_threshold = 0;
+  std::uint32_t stripes_setting = 0; // 0: automatic
+  std::uint32_t stripe_wanted = 0;
+  DeviceBuffer stripe_order;
+  cudaStream_t copy_in = nullptr, copy_out = nullptr;
+  cudaEvent_t arrived[kMaxStripes] = {}, computed[kMaxStripes] = {};
+  cudaEvent_t stripe_timing[8] = {};
+  // Prefix offsets of each instance's slice (count + 1 entries).
+  std::vector<std::uint64_t> off_nodes, off_edges, off_obs;
+  bool shared_edge_input = false;
 
   // Device data.
   DeviceBuffer node_in, edge_in, observations, root_potential, emission;
@@ -164,18 +212,31 @@ struct Workspace {
   cudaStream_t stream = nullptr;
   cudaEvent_t events[6] = {};
   int sms = 1;
-  int occupancy[3] = {1, 1, 1};
+  // Resident CTAs per SM: linear forward, maximum, sample, linear adjoint.
+  int occupancy[4] = {1, 1, 1, 1};
 
   ~Workspace() { Clear(); }
+
+  void DropGraphs() noexcept {
+    for (Graph &graph : graphs)
+      static_cast<void>(cudaGraphExecDestroy(graph.exec));
+    graphs.clear();
+  }
 
   void Clear() noexcept {
     if (stream != nullptr) {
       static_cast<void>(cudaSetDevice(device));
       static_cast<void>(cudaStreamSynchronize(stream));
     }
+    DropGraphs();
+    sorted_nodes.clear();
+    team_threshold = 0;
+    std::fill(std::begin(cta_cap), std::end(cta_cap), 0);
+    tuned_ms = 0.0f;
     for (DeviceBuffer *buffer :
          {&programs, &steps, &rakes, &combines, &absorbs, &compress, &instances,
-          &compress_ends, &gathers, &big_items, &small_items, &control, &node_in, &edge_in,
+          &compress_ends, &gathers, &team_order, &stripe_order, &control, &node_in,
+          &edge_in,
           &observations, &root_potential, &emission, &uniforms, &values,
           &node_out, &edge_out, &states_out, &scratch, &bytes})
       buffer->Free();
@@ -184,14 +245,28 @@ struct Workspace {
           &h_uniforms, &h_values, &h_node_out, &h_edge_out, &h_states,
           &h_control})
       buffer->Free();
-    for (cudaEvent_t &event : events) {
-      if (event != nullptr)
-        static_cast<void>(cudaEventDestroy(event));
-      event = nullptr;
+    for (cudaEvent_t *group : {events, arrived, computed, stripe_timing}) {
+      const std::size_t n = group == events ? 6 : group == stripe_timing ? 8 : kMaxStripes;
+      for (std::size_t i = 0; i < n; ++i) {
+        if (group[i] != nullptr)
+          static_cast<void>(cudaEventDestroy(group[i]));
+        group[i] = nullptr;
+      }
     }
-    if (stream != nullptr)
-      static_cast<void>(cudaStreamDestroy(stream));
-    stream = nullptr;
+    for (cudaStream_t *s : {&stream, &copy_in, &copy_out}) {
+      if (*s != nullptr)
+        static_cast<void>(cudaStreamDestroy(*s));
+      *s = nullptr;
+    }
+    stripe_plan.clear();
+    stripe_batch = 0;
+    stripe_threshold = 0;
+    stripes_setting = 0;
+    stripe_wanted = 0;
+    off_nodes.clear();
+    off_edges.clear();
+    off_obs.clear();
+    shared_edge_input = false;
     reserved = forest = false;
     plan = nullptr;
     states = capacity = 0;
@@ -227,6 +302,18 @@ struct Workspace {
     Check(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking),
           "cudaStreamCreateWithFlags");
     for (cudaEvent_t &event : events)
+      Check(cudaEventCreate(&event), "cudaEventCreate");
+    Check(cudaStreamCreateWithFlags(&copy_in, cudaStreamNonBlocking),
+          "cudaStreamCreateWithFlags");
+    Check(cudaStreamCreateWithFlags(&copy_out, cudaStreamNonBlocking),
+          "cudaStreamCreateWithFlags");
+    for (std::uint32_t c = 0; c < kMaxStripes; ++c) {
+      Check(cudaEventCreateWithFlags(&arrived[c], cudaEventDisableTiming),
+            "cudaEventCreate");
+      Check(cudaEventCreateWithFlags(&computed[c], cudaEventDisableTiming),
+            "cudaEventCreate");
+    }
+    for (cudaEvent_t &event : stripe_timing)
       Check(cudaEventCreate(&event), "cudaEventCreate");
     states = state_count;
     scalar = static_cast<int>(scalar_bytes);
@@ -298,21 +385,30 @@ struct Workspace {
     total_edges_out = edge_base;
     edge_inputs = shared_edges ? instance_plans.front()->num_edges() : edge_base;
     total_observations = obs_base;
+    shared_edge_input = shared_edges;
+    off_nodes.resize(count + 1);
+    off_edges.resize(count + 1);
+    off_obs.resize(count + 1);
+    for (std::size_t i = 0; i < count; ++i) {
+      off_nodes[i] = table[i].node_base;
+      off_edges[i] = table[i].edge_out_base;
+      off_obs[i] = table[i].obs_base;
+    }
+    off_nodes[count] = total_nodes;
+    off_edges[count] = total_edges_out;
+    off_obs[count] = total_observations;
 
-    // Work queues: large instances go to whole-CTA teams, small ones to
-    // single-warp teams; both ordered largest first.
-    const std::uint64_t threshold = static_cast<std::uint64_t>(TeamThreshold());
+    // Work queue: instances largest first; a prefix goes to whole-CTA teams,
+    // the rest to single-warp teams (ApplyThreshold).
     std::vector<std::uint32_t> order(count);
     std::iota(order.begin(), order.end(), 0u);
     std::stable_sort(order.begin(), order.end(), [&](std::uint32_t a, std::uint32_t b) {
       return tree_nodes[a] > tree_nodes[b];
     });
-    std::vector<std::uint32_t> big, small;
-    for (const std::uint32_t i : order)
-      (tree_nodes[i] >= threshold ? big : small).push_back(i);
-    big_count = static_cast<std::uint32_t>(big.size());
-    small_count = static_cast<std::uint32_t>(small.size());
-    items_big = !big.empty();
+    sorted_nodes.resize(count);
+    for (std::size_t i = 0; i < count; ++i)
+      sorted_nodes[i] = tree_nodes[order[i]];
+    ApplyThreshold(static_cast<std::uint32_t>(TeamThreshold()));
 
     programs.Upload(set.programs, stream);
     steps.Upload(set.steps, stream);
@@ -323,9 +419,10 @@ struct Workspace {
     compress_ends.Upload(set.compress_ends, stream);
     gathers.Upload(set.gathers, stream);
     instances.Upload(table, stream);
-    big_items.Upload(big, stream);
-    small_items.Upload(small, stream);
-    control.Allocate(16);
+    team_order.Upload(order, stream);
+    // Work counters of the forward [0..1] and adjoint [4..5] launches; [2] is
+    // the error word; words 8 + 8c .. 15 + 8c hold the counters of stripe c.
+    control.Allocate((8 + 8 * kMaxStripes) * sizeof(std::uint32_t));
 
     // Inputs, outputs and scratch.
     const std::size_t S = ScalarBytes();
@@ -366,10 +463,13 @@ struct Workspace {
     // Occupancy of each kernel this workspace may launch.
     const unsigned kmax = PaddedStates(states);
     EngineArgs probe{};
-    occupancy[0] = occupancy[1] = occupancy[2] = 1;
-    Check(scalar == 8 ? LaunchLinearF64(compute_f64, kmax, probe, 0, nullptr, &occupancy[0])
-                      : LaunchLinearF32(compute_f64, kmax, probe, 0, nullptr, &occupancy[0]),
-          "occupancy query");
+    occupancy[0] = occupancy[1] = occupancy[2] = occupancy[3] = 1;
+    for (int part = 0; part < (marginals ? 2 : 1); ++part) {
+      int *slot = &occupancy[part == 0 ? 0 : 3];
+      Check(scalar == 8 ? LaunchLinearF64(compute_f64, kmax, part, probe, 0, nullptr, slot)
+                        : LaunchLinearF32(compute_f64, kmax, part, probe, 0, nullptr, slot),
+            "occupancy query");
+    }
     if (maximum)
       Check(LaunchMaximum(scalar, kmax, probe, 0, nullptr, &occupancy[1]),
             "occupancy query");
@@ -482,15 +582,19 @@ struct Workspace {
   }
 
   // ------------------------------------------------------------------- run
+  // Which per-instance slice of a buffer a stripe owns.
+  enum Slice : int { kWhole, kNodes, kEdges, kObservations };
   struct Upload {
     const void *source;
     HostBuffer *staging;
     DeviceBuffer *device;
     std::size_t bytes;
+    Slice slice = kWhole; // kWhole: copied with the first stripe
+    std::size_t unit = 0; // bytes per node, edge or observation
   };
 
-  void EnqueueDevice(int operation, std::size_t batch) {
-    const unsigned kmax = PaddedStates(states);
+  // Kernel arguments of `operation`, without the work queue.
+  EngineArgs MakeArgs(int operation) const {
     EngineArgs args{};
     args.programs = programs.as<DevProgram>();
     args.steps = steps.as<DevStep>();
@@ -501,16 +605,6 @@ struct Workspace {
     args.compress_ends = compress_ends.ptr;
     args.gathers = gathers.ptr;
     args.instances = instances.as<DevInstance>();
-    args.big_items = big_items.as<std::uint32_t>();
-    args.small_items = small_items.as<std::uint32_t>();
-    if (forest) {
-      args.big_count = big_count;
-      args.small_count = small_count;
-    } else {
-      args.big_count = items_big ? static_cast<std::uint32_t>(batch) : 0u;
-      args.small_count = items_big ? 0u : static_cast<std::uint32_t>(batch);
-    }
-    args.queue = control.as<std::uint32_t>();
     args.error = control.as<std::uint32_t>() + 2;
     args.node_in = node_in.ptr;
     args.observations = observations.as<std::uint8_t>();
@@ -529,29 +623,197 @@ struct Workspace {
     args.edge_out = edge_out.ptr;
     args.states_out = states_out.as<std::uint32_t>();
     args.uniforms = uniforms.ptr;
+    return args;
+  }
 
+  // Launches the kernels of `operation` over the queue set in `args`, with
+  // work counters at counters[0..1] (forward) and counters[4..5] (adjoint);
+  // the counters must be zero. Returns the number of kernel launches.
+  int LaunchTeams(int operation, EngineArgs args, std::uint32_t *counters) {
+    const unsigned kmax = PaddedStates(states);
+    args.queue = counters;
     const int kind = operation == THMM_OP_MAXIMUM ? 1
                      : operation == THMM_OP_SAMPLE ? 2
                                                    : 0;
     const std::uint64_t teams_needed =
         std::max<std::uint64_t>(args.big_count, (args.small_count + kWarpsPerCta - 1) /
                                                     kWarpsPerCta);
-    const int grid = static_cast<int>(std::max<std::uint64_t>(
-        1, std::min<std::uint64_t>(teams_needed,
-                                   static_cast<std::uint64_t>(sms) *
-                                       std::max(occupancy[kind], 1))));
-    Check(cudaMemsetAsync(control.ptr, 0, 16, stream), "cudaMemsetAsync");
+    const auto grid_for = [&](int slot) {
+      int per_sm = std::max(occupancy[slot], 1);
+      if (cta_cap[slot] > 0)
+        per_sm = std::min(per_sm, cta_cap[slot]);
+      return static_cast<int>(std::max<std::uint64_t>(
+          1, std::min<std::uint64_t>(teams_needed,
+                                     static_cast<std::uint64_t>(sms) * per_sm)));
+    };
     cudaError_t status;
-    if (kind == 1)
-      status = LaunchMaximum(scalar, kmax, args, grid, stream, nullptr);
-    else if (kind == 2)
-      status = LaunchSample(scalar, kmax, args, grid, stream, nullptr);
-    else if (scalar == 8)
-      status = LaunchLinearF64(compute_f64, kmax, args, grid, stream, nullptr);
-    else
-      status = LaunchLinearF32(compute_f64, kmax, args, grid, stream, nullptr);
+    int count = 1;
+    if (kind == 1) {
+      status = LaunchMaximum(scalar, kmax, args, grid_for(1), stream, nullptr);
+    } else if (kind == 2) {
+      status = LaunchSample(scalar, kmax, args, grid_for(2), stream, nullptr);
+    } else {
+      const auto linear = [&](int part, int grid) {
+        return scalar == 8
+                   ? LaunchLinearF64(compute_f64, kmax, part, args, grid, stream, nullptr)
+                   : LaunchLinearF32(compute_f64, kmax, part, args, grid, stream, nullptr);
+      };
+      status = linear(0, grid_for(0));
+      if (status == cudaSuccess && args.reverse) {
+        args.queue = counters + 4;
+        status = linear(1, grid_for(3));
+        count = 2;
+      }
+    }
     Check(status, "tree-HMM accelerator kernel launch");
-    launches = 1;
+    return count;
+  }
+
+  // One device step over all instances of the batch, on the workspace stream.
+  void EnqueueDevice(int operation, std::size_t batch) {
+    EngineArgs args = MakeArgs(operation);
+    args.big_items = team_order.as<std::uint32_t>();
+    args.small_items = team_order.as<std::uint32_t>() + big_count;
+    if (forest) {
+      args.big_count = big_count;
+      args.small_count = small_count;
+    } else {
+      args.big_count = items_big ? static_cast<std::uint32_t>(batch) : 0u;
+      args.small_count = items_big ? 0u : static_cast<std::uint32_t>(batch);
+    }
+    Check(cudaMemsetAsync(control.ptr, 0, 32, stream), "cudaMemsetAsync");
+    launches = static_cast<std::uint64_t>(
+        LaunchTeams(operation, args, control.as<std::uint32_t>()));
+  }
+
+  // Splits the largest-first queue at `threshold` nodes (CTA teams above).
+  void ApplyThreshold(std::uint32_t threshold) {
+    team_threshold = std::max<std::uint32_t>(threshold, 1);
+    const auto split = std::partition_point(
+        sorted_nodes.begin(), sorted_nodes.end(),
+        [&](std::uint64_t n) { return n >= team_threshold; });
+    big_count = static_cast<std::uint32_t>(split - sorted_nodes.begin());
+    small_count = static_cast<std::uint32_t>(sorted_nodes.end() - split);
+    items_big = big_count != 0;
+    DropGraphs();
+  }
+
+  // Device-only step replayed from a CUDA graph captured on first use (the
+  // memset of the work counters plus the kernel launches of EnqueueDevice).
+  void EnqueueGraph(int operation, std::size_t batch) {
+    for (const Graph &graph : graphs)
+      if (graph.operation == operation && graph.batch == batch) {
+        Check(cudaGraphLaunch(graph.exec, stream), "cudaGraphLaunch");
+        return;
+      }
+    cudaGraph_t graph = nullptr;
+    Check(cudaStreamBeginCapture(stream, cudaStreamCaptureModeRelaxed),
+          "cudaStreamBeginCapture");
+    try {
+      EnqueueDevice(operation, batch);
+    } catch (...) {
+      static_cast<void>(cudaStreamEndCapture(stream, &graph));
+      if (graph != nullptr)
+        static_cast<void>(cudaGraphDestroy(graph));
+      throw;
+    }
+    Check(cudaStreamEndCapture(stream, &graph), "cudaStreamEndCapture");
+    cudaGraphExec_t exec = nullptr;
+    const cudaError_t status = cudaGraphInstantiate(&exec, graph, 0);
+    static_cast<void>(cudaGraphDestroy(graph));
+    Check(status, "cudaGraphInstantiate");
+    graphs.push_back({operation, batch, exec});
+    Check(cudaGraphLaunch(exec, stream), "cudaGraphLaunch");
+  }
+
+  static int KernelSlot(int operation) {
+    return operation == THMM_OP_MAXIMUM ? 1 : operation == THMM_OP_SAMPLE ? 2 : 0;
+  }
+
+  // Mean device time of `repeats` steps of `operation` on the resident
+  // inputs, after one untimed step.
+  float TimeSteps(int operation, int repeats) {
+    EnqueueDevice(operation, last_batch);
+    Check(cudaEventRecord(events[0], stream), "cudaEventRecord");
+    for (int r = 0; r < repeats; ++r)
+      EnqueueDevice(operation, last_batch);
+    Check(cudaEventRecord(events[1], stream), "cudaEventRecord");
+    Check(cudaEventSynchronize(events[1]), "autotune step");
+    float ms = 0.0f;
+    Check(cudaEventElapsedTime(&ms, events[0], events[1]), "cudaEventElapsedTime");
+    return ms / static_cast<float>(repeats);
+  }
+
+  // Searches the team threshold and the CTAs per SM of the kernels that
+  // `operation` launches, timing each candidate on the resident inputs, and
+  // keeps the fastest. Candidates that give the same team split are timed
+  // once.
+  thmm_tuning Autotune(int operation, int repeats) {
+    const int slot = KernelSlot(operation);
+    const bool adjoint = operation == THMM_OP_MARGINALS;
+    std::vector<std::uint32_t> thresholds;
+    std::vector<std::uint32_t> splits;
+    for (std::uint32_t t : {256u, 512u, 1024u, 2048u, 4096u, 8192u, 16384u, 1u << 31}) {
+      const auto split = static_cast<std::uint32_t>(
+          std::partition_point(sorted_nodes.begin(), sorted_nodes.end(),
+                               [&](std::uint64_t n) { return n >= t; }) -
+          sorted_nodes.begin());
+      if (std::find(splits.begin(), splits.end(), split) == splits.end()) {
+        splits.push_back(split);
+        thresholds.push_back(t);
+      }
+    }
+    const auto caps_for = [&](int s) {
+      std::vector<int> caps;
+      for (int c = std::max(occupancy[s], 1); c >= 1 && caps.size() < 3; --c)
+        caps.push_back(c);
+      return caps;
+    };
+    const std::vector<int> forward_caps = caps_for(slot);
+    const std::vector<int> reverse_caps = adjoint ? caps_for(3) : std::vector<int>{0};
+    thmm_tuning best{};
+    best.kernel_ms = std::numeric_limits<float>::infinity();
+    std::uint32_t tried = 0;
+    for (const std::uint32_t threshold : thresholds) {
+      ApplyThreshold(threshold);
+      for (const int forward : forward_caps) {
+        for (const int reverse : reverse_caps) {
+          cta_cap[slot] = forward;
+          cta_cap[3] = reverse;
+          const float ms = TimeSteps(operation, repeats);
+          ++tried;
+          if (ms < best.kernel_ms) {
+            best.kernel_ms = ms;
+            best.team_threshold = threshold;
+            std::fill(std::begin(best.ctas_per_sm), std::end(best.ctas_per_sm), 0u);
+            best.ctas_per_sm[slot] = static_cast<std::uint32_t>(forward);
+            best.ctas_per_sm[3] = static_cast<std::uint32_t>(reverse);
+          }
+        }
+      }
+    }
+    best.candidates = tried;
+    best.stripes = stripes_setting;
+    ApplyTuning(best);
+    return best;
+  }
+
+  void ApplyTuning(const thmm_tuning &tuning) {
+    ApplyThreshold(tuning.team_threshold);
+    for (int slot = 0; slot < 4; ++slot)
+      cta_cap[slot] = static_cast<int>(tuning.ctas_per_sm[slot]);
+    stripes_setting = std::min(tuning.stripes, kMaxStripes);
+    tuned_ms = tuning.kernel_ms;
+  }
+
+  thmm_tuning CurrentTuning() const {
+    thmm_tuning tuning{};
+    tuning.team_threshold = team_threshold;
+    for (int slot = 0; slot < 4; ++slot)
+      tuning.ctas_per_sm[slot] = static_cast<std::uint32_t>(cta_cap[slot]);
+    tuning.stripes = stripes_setting;
+    tuning.kernel_ms = tuned_ms;
+    return tuning;
   }
 
   struct Outcome {
@@ -565,6 +827,8 @@ struct Workspace {
     for (const Upload &upload : uploads)
       if (upload.source != upload.staging->ptr && upload.bytes != 0)
         std::memcpy(upload.staging->ptr, upload.source, upload.bytes);
+    if (StripeCount(batch) > 1)
+      return RunStriped(operation, batch, uploads, wall_start);
     Check(cudaEventRecord(events[0], stream), "cudaEventRecord");
     for (const Upload &upload : uploads)
       if (upload.bytes != 0)
@@ -599,6 +863,171 @@ struct Workspace {
     Check(cudaEventElapsedTime(&upload_ms, events[0], events[1]), "cudaEventElapsedTime");
     Check(cudaEventElapsedTime(&kernel_ms, events[2], events[3]), "cudaEventElapsedTime");
     Check(cudaEventElapsedTime(&download_ms, events[4], events[5]), "cudaEventElapsedTime");
+    Outcome outcome{};
+    outcome.timings.upload_ms = upload_ms;
+    outcome.timings.kernel_ms = kernel_ms;
+    outcome.timings.download_ms = download_ms;
+    outcome.error = h_control.as<std::uint32_t>()[2];
+    outcome.timings.wall_ms =
+        std::chrono::duration<double, std::milli>(Clock::now() - wall_start).count();
+    return outcome;
+  }
+
+  // ------------------------------------------------------ striped calls
+  std::uint32_t StripeCount(std::size_t batch) const {
+    const std::size_t items = forest ? capacity : batch;
+    std::uint64_t want = stripes_setting;
+    if (want == 0)
+      want = std::clamp<std::uint64_t>(NodesFor(batch) / kNodesPerStripe, 1, kMaxStripes);
+    return static_cast<std::uint32_t>(
+        std::min<std::uint64_t>({want, items, kMaxStripes}));
+  }
+
+  // Cuts instances [0, items) into stripes of about equal node count and
+  // uploads each stripe's largest-first order.
+  void PlanStripes(std::size_t batch, std::uint32_t wanted) {
+    const std::size_t items = forest ? capacity : batch;
+    if (stripe_batch == batch && stripe_threshold == team_threshold &&
+        stripe_wanted == wanted && !stripe_plan.empty())
+      return;
+    std::vector<std::uint32_t> bounds{0};
+    const std::uint64_t total = off_nodes[items];
+    for (std::uint32_t c = 1; c < wanted; ++c) {
+      const std::uint64_t target = total * c / wanted;
+      const auto at = std::lower_bound(off_nodes.begin(), off_nodes.begin() + items + 1,
+                                       target) - off_nodes.begin();
+      const auto index = static_cast<std::uint32_t>(at);
+      if (index > bounds.back() && index < items)
+        bounds.push_back(index);
+    }
+    bounds.push_back(static_cast<std::uint32_t>(items));
+    std::vector<std::uint32_t> order(items);
+    stripe_plan.clear();
+    for (std::size_t c = 0; c + 1 < bounds.size(); ++c) {
+      const std::uint32_t a = bounds[c], b = bounds[c + 1];
+      std::iota(order.begin() + a, order.begin() + b, a);
+      std::stable_sort(order.begin() + a, order.begin() + b,
+                       [&](std::uint32_t x, std::uint32_t y) {
+                         return tree_nodes[x] > tree_nodes[y];
+                       });
+      std::uint32_t big = 0;
+      while (a + big < b && tree_nodes[order[a + big]] >= team_threshold)
+        ++big;
+      stripe_plan.push_back({a, b, big, (b - a) - big});
+    }
+    stripe_order.Upload(order, stream);
+    stripe_batch = batch;
+    stripe_threshold = team_threshold;
+    stripe_wanted = wanted;
+  }
+
+  // Byte range [offset, offset + size) of a buffer owned by instances [a, b).
+  std::pair<std::size_t, std::size_t> SliceRange(Slice slice, std::size_t unit,
+                                                 std::size_t bytes, std::uint32_t a,
+                                                 std::uint32_t b, bool first) const {
+    const std::vector<std::uint64_t> *offsets =
+        slice == kNodes ? &off_nodes : slice == kEdges ? &off_edges
+        : slice == kObservations ? &off_obs : nullptr;
+    if (offsets == nullptr)
+      return {0, first ? bytes : 0};
+    return {(*offsets)[a] * unit, ((*offsets)[b] - (*offsets)[a]) * unit};
+  }
+
+  // A prepared call cut into stripes: per stripe, input copies on copy_in,
+  // kernels on the workspace stream after that stripe's inputs arrived, and
+  // output copies on copy_out after its kernels. Timings: upload_ms spans the
+  // input copies, kernel_ms the kernels, download_ms the output copies; they
+  // overlap.
+  Outcome RunStriped(int operation, std::size_t batch, const std::vector<Upload> &uploads,
+                     Clock::time_point wall_start) {
+    PlanStripes(batch, StripeCount(batch));
+    const auto P = static_cast<std::uint32_t>(stripe_plan.size());
+    const std::size_t S = ScalarBytes();
+    const std::size_t K = states;
+    cudaEvent_t *t = stripe_timing;
+    Check(cudaEventRecord(t[0], stream), "cudaEventRecord");
+    Check(cudaStreamWaitEvent(copy_in, t[0], 0), "cudaStreamWaitEvent");
+    Check(cudaStreamWaitEvent(copy_out, t[0], 0), "cudaStreamWaitEvent");
+    Check(cudaMemsetAsync(control.ptr, 0, (8 + 8 * P) * sizeof(std::uint32_t), stream),
+          "cudaMemsetAsync");
+    const auto device_bytes = [](DeviceBuffer &buffer) {
+      return static_cast<unsigned char *>(buffer.ptr);
+    };
+    const auto host_bytes = [](HostBuffer &buffer) {
+      return static_cast<unsigned char *>(buffer.ptr);
+    };
+    for (std::uint32_t c = 0; c < P; ++c) {
+      const Stripe &stripe = stripe_plan[c];
+      for (const Upload &upload : uploads) {
+        const auto [offset, size] = SliceRange(upload.slice, upload.unit, upload.bytes,
+                                               stripe.first, stripe.last, c == 0);
+        if (size != 0)
+          Check(cudaMemcpyAsync(device_bytes(*upload.device) + offset,
+                                host_bytes(*upload.staging) + offset, size,
+                                cudaMemcpyHostToDevice, copy_in),
+                "cudaMemcpyAsync input upload");
+      }
+      Check(cudaEventRecord(arrived[c], copy_in), "cudaEventRecord");
+    }
+    Check(cudaEventRecord(t[1], copy_in), "cudaEventRecord");
+    const EngineArgs base = MakeArgs(operation);
+    std::uint64_t count = 0;
+    for (std::uint32_t c = 0; c < P; ++c) {
+      const Stripe &stripe = stripe_plan[c];
+      Check(cudaStreamWaitEvent(stream, arrived[c], 0), "cudaStreamWaitEvent");
+      if (c == 0)
+        Check(cudaEventRecord(t[2], stream), "cudaEventRecord");
+      EngineArgs args = base;
+      args.big_items = stripe_order.as<std::uint32_t>() + stripe.first;
+      args.big_count = stripe.big;
+      args.small_items = stripe_order.as<std::uint32_t>() + stripe.first + stripe.big;
+      args.small_count = stripe.small;
+      count += static_cast<std::uint64_t>(
+          LaunchTeams(operation, args, control.as<std::uint32_t>() + 8 + 8 * c));
+      Check(cudaEventRecord(computed[c], stream), "cudaEventRecord");
+    }
+    Check(cudaEventRecord(t[3], stream), "cudaEventRecord");
+    const auto download = [&](HostBuffer &host, DeviceBuffer &dev, Slice slice,
+                              std::size_t unit, const Stripe &stripe) {
+      std::size_t offset, size;
+      if (slice == kWhole) {
+        offset = stripe.first * unit;
+        size = (stripe.last - stripe.first) * unit;
+      } else {
+        std::tie(offset, size) = SliceRange(slice, unit, 0, stripe.first, stripe.last,
+                                            false);
+      }
+      if (size != 0)
+        Check(cudaMemcpyAsync(host_bytes(host) + offset, device_bytes(dev) + offset, size,
+                              cudaMemcpyDeviceToHost, copy_out),
+              "cudaMemcpyAsync result download");
+    };
+    for (std::uint32_t c = 0; c < P; ++c) {
+      const Stripe &stripe = stripe_plan[c];
+      Check(cudaStreamWaitEvent(copy_out, computed[c], 0), "cudaStreamWaitEvent");
+      if (c == 0)
+        Check(cudaEventRecord(t[4], copy_out), "cudaEventRecord");
+      download(h_values, values, kWhole, S, stripe); // one value per instance
+      if (operation == THMM_OP_MARGINALS) {
+        download(h_node_out, node_out, kNodes, K * S, stripe);
+        download(h_edge_out, edge_out, kEdges, K * K * S, stripe);
+      }
+      if (operation == THMM_OP_MAXIMUM || operation == THMM_OP_SAMPLE)
+        download(h_states, states_out, kNodes, sizeof(std::uint32_t), stripe);
+    }
+    Check(cudaMemcpyAsync(h_control.ptr, control.ptr, 16, cudaMemcpyDeviceToHost, copy_out),
+          "cudaMemcpyAsync result download");
+    Check(cudaEventRecord(t[5], copy_out), "cudaEventRecord");
+    // Later work on the workspace stream follows this call's downloads.
+    Check(cudaStreamWaitEvent(stream, t[5], 0), "cudaStreamWaitEvent");
+    Check(cudaEventSynchronize(t[5]), "tree-HMM accelerator execution");
+    launches = count;
+    last_batch = batch;
+    has_run = true;
+    float upload_ms = 0, kernel_ms = 0, download_ms = 0;
+    Check(cudaEventElapsedTime(&upload_ms, t[0], t[1]), "cudaEventElapsedTime");
+    Check(cudaEventElapsedTime(&kernel_ms, t[2], t[3]), "cudaEventElapsedTime");
+    Check(cudaEventElapsedTime(&download_ms, t[4], t[5]), "cudaEventElapsedTime");
     Outcome outcome{};
     outcome.timings.upload_ms = upload_ms;
     outcome.timings.kernel_ms = kernel_ms;
@@ -678,11 +1107,18 @@ void CheckDense(const Workspace &ws, const thmm_dense_model &model,
     throw std::invalid_argument("accelerator edge input shape is wrong");
 }
 
+Workspace::Slice EdgeSlice(const Workspace &ws) {
+  return ws.shared_edge_input ? Workspace::kWhole : Workspace::kEdges;
+}
+
 std::vector<Workspace::Upload> DenseUploads(Workspace &ws,
                                             const thmm_dense_model &model) {
   const std::size_t S = ws.ScalarBytes();
-  return {{model.node_potentials, &ws.h_node_in, &ws.node_in, model.node_count * S},
-          {model.edge_potentials, &ws.h_edge_in, &ws.edge_in, model.edge_count * S}};
+  const std::size_t K = ws.states;
+  return {{model.node_potentials, &ws.h_node_in, &ws.node_in, model.node_count * S,
+           Workspace::kNodes, K * S},
+          {model.edge_potentials, &ws.h_edge_in, &ws.edge_in, model.edge_count * S,
+           EdgeSlice(ws), K * K * S}};
 }
 
 // Categorical checks and residency rules (src/gpu_backend_impl.inc:2842-2946).
@@ -695,9 +1131,10 @@ std::vector<Workspace::Upload> CategoricalUploads(Workspace &ws,
       model.observation_node_count != ws.observation_nodes.size() ||
       (model.observation_node_count != 0 &&
        (model.observation_nodes == nullptr ||
-        !std::equal(model.observation_nodes,
-                    model.observation_nodes + model.observation_node_count,
-                    ws.observation_nodes.begin()))))
+        (model.observation_nodes != ws.observation_nodes.data() &&
+         !std::equal(model.observation_nodes,
+                     model.observation_nodes + model.observation_node_count,
+                     ws.observation_nodes.begin())))))
     throw std::invalid_argument(
         "categorical accelerator model does not match the reserved workspace");
   if (update != THMM_UPDATE_ALL && update != THMM_UPDATE_FACTORS &&
@@ -728,14 +1165,14 @@ std::vector<Workspace::Upload> CategoricalUploads(Workspace &ws,
   std::vector<Workspace::Upload> uploads;
   if (update_observations)
     uploads.push_back({model.observations, &ws.h_observations, &ws.observations,
-                       model.observation_count});
+                       model.observation_count, Workspace::kObservations, 1});
   if (update_factors) {
     uploads.push_back({model.root_potential, &ws.h_root, &ws.root_potential,
                        model.root_count * S});
     uploads.push_back({model.emission_potentials, &ws.h_emission, &ws.emission,
                        model.emission_count * S});
     uploads.push_back({model.edge_potentials, &ws.h_edge_in, &ws.edge_in,
-                       model.edge_count * S});
+                       model.edge_count * S, EdgeSlice(ws), ws.states * ws.states * S});
   }
   return uploads;
 }
@@ -754,7 +1191,8 @@ std::vector<Workspace::Upload> UniformUpload(Workspace &ws, std::size_t batch,
     throw std::invalid_argument(
         "prepared accelerator posterior sampling requires ReserveSampling and "
         "one uniform variate per batch item and node");
-  return {{uniforms, &ws.h_uniforms, &ws.uniforms, count * ws.ScalarBytes()}};
+  return {{uniforms, &ws.h_uniforms, &ws.uniforms, count * ws.ScalarBytes(),
+           Workspace::kNodes, ws.ScalarBytes()}};
 }
 
 void CheckSamplingOutcome(const Workspace &ws, const Workspace::Outcome &outcome,
@@ -1183,9 +1621,52 @@ thmm_status thmm_enqueue(thmm_workspace *workspace, int operation,
         (operation == THMM_OP_MARGINALS && !ws.marginals))
       throw std::invalid_argument("operation was not reserved");
     thmm::Check(cudaSetDevice(ws.device), "cudaSetDevice");
-    ws.EnqueueDevice(operation, ws.last_batch);
+    ws.EnqueueGraph(operation, ws.last_batch);
     if (nodes_out != nullptr)
       *nodes_out = ws.NodesFor(ws.last_batch);
+  });
+}
+
+thmm_status thmm_autotune(thmm_workspace *workspace, int operation, int repeats,
+                          thmm_tuning *out) {
+  return Guard([&] {
+    Workspace &ws = thmm::AsWorkspace(workspace);
+    if (!ws.reserved || !ws.has_run)
+      throw std::logic_error(
+          "thmm_autotune needs inputs left resident by a prepared call");
+    if (operation < THMM_OP_PARTITION || operation > THMM_OP_MARGINALS)
+      throw std::invalid_argument("unknown operation");
+    if ((operation == THMM_OP_MAXIMUM && !ws.maximum) ||
+        (operation == THMM_OP_SAMPLE && !ws.sampling) ||
+        (operation == THMM_OP_MARGINALS && !ws.marginals))
+      throw std::invalid_argument("operation was not reserved");
+    if (repeats < 1)
+      throw std::invalid_argument("autotune needs at least one timed repeat");
+    thmm::Check(cudaSetDevice(ws.device), "cudaSetDevice");
+    const thmm_tuning tuning = ws.Autotune(operation, repeats);
+    if (out != nullptr)
+      *out = tuning;
+  });
+}
+
+thmm_status thmm_get_tuning(const thmm_workspace *workspace, thmm_tuning *out) {
+  return Guard([&] {
+    if (workspace == nullptr || out == nullptr)
+      throw std::invalid_argument("workspace and result must not be null");
+    *out = reinterpret_cast<const Workspace *>(workspace)->CurrentTuning();
+  });
+}
+
+thmm_status thmm_set_tuning(thmm_workspace *workspace, const thmm_tuning *tuning) {
+  return Guard([&] {
+    Workspace &ws = thmm::AsWorkspace(workspace);
+    if (tuning == nullptr)
+      throw std::invalid_argument("tuning must not be null");
+    if (!ws.reserved)
+      throw std::logic_error("thmm_set_tuning needs a reserved workspace");
+    if (tuning->team_threshold == 0)
+      throw std::invalid_argument("team threshold must be positive");
+    ws.ApplyTuning(*tuning);
   });
 }
 

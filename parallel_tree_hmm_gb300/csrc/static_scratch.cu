@@ -141,7 +141,7 @@ DeviceSetup &Setup(int device) {
     const unsigned kmax[4] = {4, 8, 16, 32};
     EngineArgs probe{};
     for (int i = 0; i < 4; ++i)
-      Check(LaunchLinearTyped<float, float>(kmax[i], probe, 0, nullptr,
+      Check(LaunchLinearTyped<float, float>(kmax[i], kLinearForward, probe, 0, nullptr,
                                             &setup.occupancy[i]),
             "occupancy query");
     setup.ready = true;
@@ -256,7 +256,7 @@ extern "C" thmm_status thmm_log_partition_static(
     const int grid = static_cast<int>(std::max<std::size_t>(
         1, std::min<std::size_t>(teams, static_cast<std::size_t>(setup.sms) *
                                             std::max(setup.occupancy[index], 1))));
-    Check(LaunchLinearTyped<float, float>(kmax, args, grid, stream, nullptr),
+    Check(LaunchLinearTyped<float, float>(kmax, kLinearForward, args, grid, stream, nullptr),
           "tree-HMM accelerator kernel launch");
     return THMM_OK;
   } catch (const std::invalid_argument &error) {

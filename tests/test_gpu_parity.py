@@ -303,7 +303,7 @@ def test_enqueue_matches_prepared_call(gpu):
     first = ws.posterior_marginals_prepared(
         gpu.BatchedModelView(plan, states, batch, nodes.ravel(), edges))
     values = first.log_partitions.copy()
-    assert ws.launches == 1
+    assert ws.launches == 2  # forward sweep, then adjoint sweep
     assert ws.enqueue(4) == batch * plan.num_nodes
     ws.synchronize()
     again = ws.posterior_marginals_prepared(
