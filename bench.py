@@ -60,7 +60,16 @@ def parse_args():
     parser.add_argument("--seed", type=int, default=0)
     parser.add_argument("--e2e-steps", type=int, default=None)
     parser.add_argument("--cpu-sample-nodes", type=int, default=20_000_000)
-    return parser.parse_args()
+    parser.add_argument("--workload", choices=["forest", "gw"], default="forest",
+                        help="forest: uneven forest, marginals (default); gw: "
+                             "Galton-Watson forest, MAP + posterior sampling")
+    args = parser.parse_args()
+    if args.workload == "gw":
+        if args.trees == 4096:
+            args.trees = 1024
+        if args.states == 4:
+            args.states = 8
+    return args
 
 
 # ------------------------------------------------------------------ workload
@@ -231,7 +240,9 @@ def main():
             torch.cuda.set_device(local_rank)
         dist.init_process_group("nccl" if args.impl == "ours" else "gloo")
 
-    if args.impl == "reference":
+    if args.workload == "gw":
+        run_gw(args, rank, world, local_rank, dist)
+    elif args.impl == "reference":
         run_reference(args, rank, world, dist)
     else:
         run_ours(args, rank, world, local_rank, dist)
@@ -451,6 +462,210 @@ def run_ours(args, rank, world, local_rank, dist):
         root, emission, edges = factor_sets[0]
         line["cpu_baseline"] = cpu_baseline(forest, root, emission, edges, observations,
                                             args.cpu_sample_nodes)
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+
+
+# ------------------------------------------------- MAP + sampling workload
+class GaltonWatsonForest:
+    """Poisson(2) Galton-Watson trees of 1,000-50,000 nodes (grown breadth
+    first to a uniform size cap), K states, byte observations on the leaves
+    with a Dirichlet(2) emission table, Dirichlet(0.3) edge rows, Dirichlet(1)
+    root factor and one U[0,1) variate per node."""
+
+    def __init__(self, trees: int, states: int, seed: int):
+        from parallel_tree_hmm_gb300 import synthetic
+
+        rng = np.random.default_rng(seed)
+        self.parents = [synthetic.galton_watson(rng) for _ in range(trees)]
+        self.states = states
+        self.observed = [synthetic.leaves(p) for p in self.parents]
+        self.num_nodes = np.array([len(p) for p in self.parents], dtype=np.int64)
+        self.total_nodes = int(self.num_nodes.sum())
+        self.total_edges = int((self.num_nodes - 1).sum())
+        self.total_observed = int(sum(len(o) for o in self.observed))
+        K = states
+        self.root = synthetic.dirichlet_rows(rng, 1, K, 1.0, np.float32).ravel()
+        self.emission = synthetic.dirichlet_rows(rng, K, K, 2.0, np.float32).ravel()
+        g = rng.standard_gamma(0.3, size=(self.total_edges * K, K), dtype=np.float32)
+        g /= g.sum(axis=1, keepdims=True)
+        np.nan_to_num(g, copy=False, nan=1.0 / K)
+        self.edges = g.ravel()
+        self.observations = rng.integers(0, K, size=self.total_observed, dtype=np.uint8)
+        self.uniforms = rng.random(self.total_nodes, dtype=np.float32)
+
+    def tree_inputs(self, t, dtype):
+        """Dense node factors, edge factors and uniforms of tree t."""
+        K = self.states
+        node0 = int(self.num_nodes[:t].sum())
+        edge0 = node0 - t
+        obs0 = int(sum(len(o) for o in self.observed[:t]))
+        n = int(self.num_nodes[t])
+        dense = np.ones((n, K), dtype=np.float64)
+        dense[0] = self.root
+        obs = self.observations[obs0:obs0 + len(self.observed[t])]
+        dense[self.observed[t]] *= self.emission.astype(np.float64).reshape(K, K)[obs]
+        if dtype == np.float32:
+            # (root ? root : 1) * emission[obs] in FP32, as the kernel forms it.
+            dense32 = np.ones((n, K), dtype=np.float32)
+            dense32[0] = self.root
+            dense32[self.observed[t]] = (dense32[self.observed[t]] *
+                                         self.emission.reshape(K, K)[obs])
+            dense = dense32
+        edges = self.edges[edge0 * K * K:(edge0 + n - 1) * K * K].astype(dtype)
+        return dense.ravel().astype(dtype), edges, self.uniforms[node0:node0 + n]
+
+
+def run_gw(args, rank, world, local_rank, dist):
+    import parallel_tree_hmm_gb300 as thmm
+    from oracle import bridge
+
+    forest = GaltonWatsonForest(args.trees, args.states, rank_seed(args.seed, rank))
+    K = forest.states
+    config = {
+        "workload": (f"Galton-Watson forest: {args.trees} Poisson(2) trees of "
+                     f"1,000-50,000 nodes, K={K}, byte leaf observations, "
+                     f"Dirichlet(0.3) edges, MAP + posterior sampling"),
+        "trees": args.trees, "nodes_per_rank": forest.total_nodes, "states": K,
+        "seed": args.seed, "parallelism": f"replicas of the forest per GPU x{args.gpus}",
+        "l2": "inputs larger than L2 (edge factors of one step > 129 MB)",
+    }
+    metric = "tree-nodes/s for MAP+posterior sampling"
+    if args.impl == "reference":
+        if rank != 0:
+            return
+        sample_trees = max(1, min(args.trees, 64))
+        per_step = []
+        for _ in range(args.warmup + args.steps):
+            start = time.perf_counter()
+            nodes = 0
+            jobs = [(t, thmm.Plan(forest.parents[t])) for t in range(sample_trees)]
+
+            def run(job):
+                t, plan = job
+                dense, edges, uniforms = forest.tree_inputs(t, np.float64)
+                bridge.maximum(plan, K, dense, edges)
+                bridge.sample(plan, K, dense, edges, uniforms.astype(np.float64))
+                return plan.num_nodes
+
+            with concurrent.futures.ThreadPoolExecutor(os.cpu_count() or 1) as pool:
+                nodes = sum(pool.map(run, jobs))
+            per_step.append(nodes / (time.perf_counter() - start))
+        value = statistics.median(per_step[args.warmup:])
+        print(json.dumps({
+            "impl": "reference", "metric": metric, "value": value, "unit": UNIT,
+            "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": None, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic", "config": config,
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": os.cpu_count() or 1,
+                             "kind": "port",
+                             "sample": f"first {sample_trees} trees, FP64 MAP + sample"},
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": 0}}), flush=True)
+        return
+
+    import torch
+
+    device = local_rank
+    torch.cuda.set_device(device)
+    plans = [thmm.Plan(p) for p in forest.parents]
+    ws = thmm.Workspace()
+    ws.reserve_forest_categorical(plans, K, K, forest.observed, device,
+                                  kind="maximum,sampling", scalar=np.float32)
+    staged = ws.categorical_inputs()
+    staged.root_potential[:] = forest.root
+    staged.emission_potentials[:] = forest.emission
+    staged.edge_potentials[:] = forest.edges
+    staged.observations[:] = forest.observations
+    uniforms = ws.uniforms()
+    uniforms[:] = forest.uniforms
+    map_view = ws.maximum_a_posteriori_prepared(staged, thmm.CategoricalInputUpdate.kAll)
+    map_states = np.array(map_view.states)
+    map_weights = np.array(map_view.log_weights)
+    sample_states = np.array(ws.posterior_sample_prepared(
+        staged, uniforms, thmm.CategoricalInputUpdate.kNone).states)
+
+    # Bit-exact check on the first trees against the oracle (FP32, reproducible
+    # exp/log) and agreement of the MAP states with the FP64 oracle.
+    check_trees = min(8, args.trees)
+    exact, agree, checked = 0, 0, 0
+    node0 = 0
+    for t in range(check_trees):
+        n = int(forest.num_nodes[t])
+        dense, edges, u = forest.tree_inputs(t, np.float32)
+        w32, s32 = bridge.maximum(plans[t], K, dense, edges, np.float32, bridge.MATH_PORTABLE)
+        draw = bridge.sample(plans[t], K, dense, edges, u, np.float32, bridge.MATH_PORTABLE)
+        exact += int(np.array_equal(s32, map_states[node0:node0 + n]) and
+                     w32 == map_weights[t] and
+                     np.array_equal(draw, sample_states[node0:node0 + n]))
+        dense64, edges64, _ = forest.tree_inputs(t, np.float64)
+        _, s64 = bridge.maximum(plans[t], K, dense64, edges64)
+        agree += int(np.sum(s64 == map_states[node0:node0 + n]))
+        checked += n
+        node0 += n
+
+    tuning_map = ws.autotune(2, repeats=2)
+    tuning_sample = ws.autotune(3, repeats=2)
+
+    def step():
+        ws.enqueue(2)
+        ws.enqueue(3)
+
+    ext = torch.cuda.ExternalStream(ws.stream, device=device)
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize(device)
+    if dist is not None:
+        dist.barrier()
+    sampler = ClockSampler(device)
+    with sampler:
+        start = torch.cuda.Event(enable_timing=True)
+        stop = torch.cuda.Event(enable_timing=True)
+        start.record(ext)
+        for _ in range(args.steps):
+            step()
+        stop.record(ext)
+        stop.synchronize()
+    elapsed_ms = reduce_max(start.elapsed_time(stop), dist)
+    step_ms = elapsed_ms / args.steps
+    value = forest.total_nodes * world / (step_ms / 1e3)
+
+    e2e_steps = args.e2e_steps or max(3, min(args.steps, 10))
+    e2e_total = 0.0
+    for _ in range(e2e_steps):
+        torch.cuda.synchronize(device)
+        begin = time.perf_counter()
+        ws.maximum_a_posteriori_prepared(staged, thmm.CategoricalInputUpdate.kFactors)
+        ws.posterior_sample_prepared(staged, uniforms, thmm.CategoricalInputUpdate.kNone)
+        e2e_total += time.perf_counter() - begin
+    e2e_total = reduce_max(e2e_total, dist)
+    S = 4
+    h2d = forest.total_edges * K * K * S + (K + K * K) * S + forest.total_nodes * S
+    d2h = 2 * forest.total_nodes * 4 + len(plans) * S + 32
+
+    algorithmic = (2 * forest.total_edges * K * K * S + 2 * forest.total_observed
+                   + forest.total_nodes * (S + 4 + 4) + len(plans) * S)
+    peaks = json.loads((ROOT / "MEASURED_PEAKS.json").read_text()) \
+        if (ROOT / "MEASURED_PEAKS.json").exists() else {}
+    peak = peaks.get("hbm_gbs", 6800.0)
+    achieved = algorithmic / (step_ms / 1e3) / 1e9
+    line = {
+        "metric": metric, "value": value, "unit": UNIT, "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": step_ms,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32", "data": "synthetic",
+        "config": {**config, "tuning_map": tuning_map, "tuning_sample": tuning_sample,
+                   "bit_exact_trees": f"{exact}/{check_trees}",
+                   "map_fp64_state_agreement": agree / checked},
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                     "frac": achieved / peak,
+                     "peak_source": "measured" if peaks else "fallback",
+                     "traffic": None, "algorithmic_bytes_per_launch": algorithmic},
+        "e2e": {"value": forest.total_nodes * world * e2e_steps / e2e_total, "unit": UNIT,
+                "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
+        "gpu_launches": 2 * args.steps,
+        "clocks": sampler.summary(),
+    }
     if rank == 0:
         print(json.dumps(line), flush=True)
 

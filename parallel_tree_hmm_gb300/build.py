@@ -35,6 +35,7 @@ SOURCES = [
     "program.cc",
     "runtime.cc",
     "engine_linear_f32.cu",
+    "engine_wide.cu",
     "engine_linear_f64.cu",
     "engine_maximum.cu",
     "engine_sample.cu",

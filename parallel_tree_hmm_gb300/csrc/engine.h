@@ -99,6 +99,7 @@ enum EngineMode : std::uint32_t {
 enum ErrorBits : std::uint32_t {
   kErrorInvalidUniform = 1u,
   kErrorEmptyConditional = 2u,
+  kErrorTensorTimeout = 4u, // a tensor-core completion wait gave up
 };
 
 struct EngineArgs {

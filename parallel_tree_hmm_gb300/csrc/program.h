@@ -55,8 +55,17 @@ cudaError_t LaunchMaximum(int scalar_bytes, unsigned kmax,
 cudaError_t LaunchSample(int scalar_bytes, unsigned kmax, const EngineArgs &args,
                          int grid, cudaStream_t stream, int *blocks_per_sm);
 
+// Tensor-core sum-product kernels for 32 < K <= 128 (kmax 64 or 128, FP32).
+cudaError_t LaunchWide(unsigned kmax, int part, const EngineArgs &args, int grid,
+                       cudaStream_t stream, int *blocks_per_sm);
+
 inline unsigned PaddedStates(std::size_t states) {
-  return states <= 4 ? 4u : states <= 8 ? 8u : states <= 16 ? 16u : 32u;
+  return states <= 4    ? 4u
+         : states <= 8  ? 8u
+         : states <= 16 ? 16u
+         : states <= 32 ? 32u
+         : states <= 64 ? 64u
+                        : 128u;
 }
 
 } // namespace thmm

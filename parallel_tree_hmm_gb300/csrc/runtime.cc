@@ -291,9 +291,16 @@ struct Workspace {
     if (state_count == 0)
       throw std::invalid_argument(
           "accelerator state and batch counts must be nonzero");
-    if (state_count > 32)
+    if (state_count > 128)
       throw std::invalid_argument(
           "state count exceeds the accelerator compression block limit");
+    // 32 < K <= 128 runs on the tensor-core sum-product engine, which takes
+    // FP32 factors and FP32 arithmetic and has no MAP or sampling kernel.
+    if (state_count > 32 &&
+        (scalar_bytes != THMM_SCALAR_F32 || (flags & THMM_COMPUTE_F64) != 0 ||
+         (flags & (THMM_RESERVE_MAXIMUM | THMM_RESERVE_SAMPLING)) != 0))
+      throw std::invalid_argument(
+          "state counts above 32 support FP32 log partitions and marginals only");
     Clear();
     device = device_index;
     Check(cudaSetDevice(device), "cudaSetDevice");
@@ -689,6 +696,8 @@ struct Workspace {
   // Splits the largest-first queue at `threshold` nodes (CTA teams above).
   void ApplyThreshold(std::uint32_t threshold) {
     team_threshold = std::max<std::uint32_t>(threshold, 1);
+    if (states > 32)
+      team_threshold = 1; // the wide-state engine contracts every tree with a CTA
     const auto split = std::partition_point(
         sorted_nodes.begin(), sorted_nodes.end(),
         [&](std::uint64_t n) { return n >= team_threshold; });
@@ -868,6 +877,8 @@ struct Workspace {
     outcome.timings.kernel_ms = kernel_ms;
     outcome.timings.download_ms = download_ms;
     outcome.error = h_control.as<std::uint32_t>()[2];
+    if (outcome.error & kErrorTensorTimeout)
+      throw std::runtime_error("tree-HMM accelerator tensor-core wait timed out");
     outcome.timings.wall_ms =
         std::chrono::duration<double, std::milli>(Clock::now() - wall_start).count();
     return outcome;
@@ -1033,6 +1044,8 @@ struct Workspace {
     outcome.timings.kernel_ms = kernel_ms;
     outcome.timings.download_ms = download_ms;
     outcome.error = h_control.as<std::uint32_t>()[2];
+    if (outcome.error & kErrorTensorTimeout)
+      throw std::runtime_error("tree-HMM accelerator tensor-core wait timed out");
     outcome.timings.wall_ms =
         std::chrono::duration<double, std::milli>(Clock::now() - wall_start).count();
     return outcome;

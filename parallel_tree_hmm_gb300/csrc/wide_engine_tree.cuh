@@ -1,0 +1,131 @@
+// Tree contraction of the wide-state engine (included by wide_engine.cuh).
+#ifndef THMM_WIDE_ENGINE_TREE_CUH_
+#define THMM_WIDE_ENGINE_TREE_CUH_
+
+namespace thmm {
+namespace wide {
+
+// One tree instance contracted by the whole CTA. Scratch layout and operation
+// records are those of the narrow engines (engine.h): node messages N*K,
+// (unused) branch slots, compressed paths C*K*K and their adjoints C*K*K.
+template <int KP> struct Tree {
+  const EngineArgs &a;
+  Shared &sh;
+  unsigned char *smem;
+  std::uint32_t tmem;
+  std::uint32_t &phase;
+  DevInstance inst;
+  DevProgram prog;
+  unsigned K, KK;
+  float *nodes;
+  float *comps;
+  float *comp_mu;
+  const float *edge_in;
+  // K-vectors in shared memory.
+  float *v, *leaf, *msg, *middle, *ratio, *spare;
+  long long exponent = 0; // thread 0's log-scale exponent sum
+  int zero = 0;           // some renormalised message was identically zero
+  bool ok = true;         // every tensor-core wait completed
+
+  __device__ Tree(const EngineArgs &args, unsigned item, Shared &shared,
+                  unsigned char *dynamic_smem, std::uint32_t tmem_base,
+                  std::uint32_t &mma_phase)
+      : a(args), sh(shared), smem(dynamic_smem), tmem(tmem_base), phase(mma_phase) {
+    inst = a.instances[item];
+    prog = a.programs[inst.program];
+    K = a.states;
+    KK = K * K;
+    float *base = static_cast<float *>(a.scratch) + inst.scratch_base;
+    nodes = base;
+    comps = nodes + static_cast<std::size_t>(prog.num_nodes) * K +
+            static_cast<std::size_t>(prog.num_rakes) * K;
+    comp_mu = comps + static_cast<std::size_t>(prog.num_compressions) * KK;
+    edge_in = static_cast<const float *>(a.edge_in) +
+              inst.edge_in_base * static_cast<std::uint64_t>(KK);
+    float *vectors = reinterpret_cast<float *>(smem + 4 * kOperandBytes);
+    v = vectors;
+    leaf = vectors + 128;
+    msg = vectors + 256;
+    middle = vectors + 384;
+    ratio = vectors + 512;
+    spare = vectors + 640;
+  }
+
+  // Row r of path version `ref` (input edge, or compressed path kFlag | t).
+  __device__ __forceinline__ const float *Path(unsigned ref) const {
+    return (ref & kFlag) ? comps + static_cast<std::size_t>(ref & kMask) * KK
+                         : edge_in + static_cast<std::size_t>(ref) * KK;
+  }
+
+  // dst[j] for j < K: the stored value of node `ref` (kFlag) or its input
+  // factor; for a categorical model (root ? root potential : 1) times the
+  // emission row of its observation (src/gpu_backend_impl.inc:326-382).
+  __device__ __forceinline__ void NodeVector(unsigned ref, unsigned obs, float *dst) const {
+    const unsigned j = threadIdx.x;
+    if (j >= K)
+      return;
+    if (ref & kFlag) {
+      dst[j] = nodes[static_cast<std::size_t>(ref & kMask) * K + j];
+      return;
+    }
+    if (!a.categorical) {
+      dst[j] = static_cast<const float *>(a.node_in)[(inst.node_base + ref) * K + j];
+      return;
+    }
+    const bool root = ref == (prog.root & kMask);
+    const float *root_potential = static_cast<const float *>(a.root_potential);
+    float value = root ? root_potential[j] : 1.0f;
+    if (obs != kNone) {
+      const unsigned category = a.observations[inst.obs_base + obs];
+      value = category < a.categories
+                  ? value * static_cast<const float *>(a.emission)[category * K + j]
+                  : 0.0f;
+    }
+    dst[j] = value;
+  }
+
+  // out[i] = sum_j path[i][j] * x[j] for i < K (x and out in shared memory).
+  __device__ __forceinline__ void MatVec(const float *path, const float *x, float *out) const {
+    const unsigned warp = threadIdx.x / 32, lane = threadIdx.x & 31;
+#pragma unroll 2
+    for (unsigned i = warp; i < K; i += kThreads / 32) {
+      const float *row = path + static_cast<std::size_t>(i) * K;
+      float s = 0.0f;
+#pragma unroll
+      for (unsigned q = 0; q < KP / 32; ++q) {
+        const unsigned j = lane + 32 * q;
+        if (j < K)
+          s = fmaf(row[j], x[j], s);
+      }
+      s = WarpSum(s);
+      if (lane == 0)
+        out[i] = s;
+    }
+  }
+
+  // Exponent of the CTA maximum m = f 2^e (f in [0.5, 1)), recorded once; a
+  // zero maximum sets the zero flag and gives 0.
+  __device__ __forceinline__ int Renormaliser(float local_max) {
+    const float m = BlockMax(local_max, sh);
+    if (m > 0.0f) {
+      const int e = Pow2Exponent(m);
+      if (threadIdx.x == 0)
+        exponent += e;
+      return e;
+    }
+    if (threadIdx.x == 0)
+      zero = 1;
+    return 0;
+  }
+
+  __device__ void Forward();
+  __device__ void Reverse();
+  __device__ void Finish(unsigned item);
+};
+
+} // namespace wide
+} // namespace thmm
+
+#include "wide_engine_sweeps.cuh"
+
+#endif // THMM_WIDE_ENGINE_TREE_CUH_

@@ -63,22 +63,23 @@ def galton_watson(rng: np.random.Generator, minimum: int = 1000,
                   maximum: int = 50000, mean: float = 2.0) -> np.ndarray:
     """Poisson(mean) Galton-Watson tree grown breadth first until a size cap
     drawn uniformly from [minimum, maximum] is reached; a tree that dies out
-    below `minimum` nodes is discarded and regrown."""
+    below `minimum` nodes is discarded and regrown.
+
+    Breadth-first growth appends the children of node 0, then of node 1, and
+    so on, so with offspring counts c_k the parent array is node k repeated
+    c_k times, in order; the tree dies out at the first node k that does not
+    exist (1 + c_0 + ... + c_{k-1} <= k)."""
     cap = int(rng.integers(minimum, maximum + 1))
     while True:
-        parents = [-1]
-        frontier = [0]
-        head = 0
-        while head < len(frontier) and len(parents) < cap:
-            node = frontier[head]
-            head += 1
-            for _ in range(int(rng.poisson(mean))):
-                if len(parents) >= cap:
-                    break
-                frontier.append(len(parents))
-                parents.append(node)
+        counts = rng.poisson(mean, size=cap)
+        born = 1 + np.cumsum(counts)  # nodes present after processing node k
+        alive = born[:-1] > np.arange(1, cap)  # node k + 1 exists
+        dead = np.flatnonzero(~alive)
+        processed = cap if dead.size == 0 else int(dead[0]) + 1
+        children = np.repeat(np.arange(processed, dtype=np.int64), counts[:processed])
+        parents = np.concatenate([[-1], children])[:cap]
         if len(parents) >= minimum:
-            return np.asarray(parents, dtype=np.int64)
+            return parents
 
 
 def dirichlet_rows(rng: np.random.Generator, rows: int, states: int,

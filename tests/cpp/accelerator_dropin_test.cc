@@ -382,8 +382,8 @@ void Residency() {
   fresh.Reserve(plan, K, 2);
   Check(Throws<std::logic_error>([&] { fresh.CategoricalInputs(1); }),
         "CategoricalInputs on a dense workspace");
-  Check(Throws<std::invalid_argument>([&] { fresh.Reserve(plan, 33, 2); }),
-        "more than 32 states");
+  Check(Throws<std::invalid_argument>([&] { fresh.Reserve(plan, 129, 2); }),
+        "more than 128 states");
 }
 
 void DenseRecovery() {

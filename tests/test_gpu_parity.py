@@ -309,3 +309,49 @@ def test_enqueue_matches_prepared_call(gpu):
     again = ws.posterior_marginals_prepared(
         gpu.BatchedModelView(plan, states, batch, nodes.ravel(), edges))
     assert np.array_equal(again.log_partitions, values)
+
+
+def test_galton_watson_categorical_map_and_sampling_bit_exact(gpu):
+    """MAP and sampling on the MAP+sampling workload's tree and factor shapes
+    (Poisson(2) Galton-Watson trees, K = 8, byte leaf observations with a
+    Dirichlet(2) emission table, Dirichlet(0.3) edge rows), categorical
+    forest, FP32: states, weights and draws bit-exact against the oracle."""
+    rng = np.random.default_rng(2024)
+    K = 8
+    parents = [synthetic.galton_watson(rng, 1000, 4000) for _ in range(3)]
+    plans = [gpu.Plan(p) for p in parents]
+    observed = [synthetic.leaves(p) for p in parents]
+    root = synthetic.dirichlet_rows(rng, 1, K, 1.0, np.float32).ravel()
+    emission = synthetic.dirichlet_rows(rng, K, K, 2.0, np.float32)
+    edges = [synthetic.dirichlet_rows(rng, (len(p) - 1) * K, K, 0.3, np.float32).ravel()
+             for p in parents]
+    obs = [rng.integers(0, K, len(o), dtype=np.uint8) for o in observed]
+    uniforms = [rng.random(len(p)).astype(np.float32) for p in parents]
+    ws = gpu.Workspace()
+    ws.reserve_forest_categorical(plans, K, K, observed, kind="maximum,sampling",
+                                  scalar=np.float32)
+    staged = ws.categorical_inputs()
+    staged.root_potential[:] = root
+    staged.emission_potentials[:] = emission.ravel()
+    staged.edge_potentials[:] = np.concatenate(edges)
+    staged.observations[:] = np.concatenate(obs)
+    u = ws.uniforms()
+    u[:] = np.concatenate(uniforms)
+    map_view = ws.maximum_a_posteriori_prepared(staged, 0)
+    # Result spans live in workspace memory until the next call: copy them.
+    map_weights, map_states = np.array(map_view.log_weights), np.array(map_view.states)
+    sample_states = np.array(ws.posterior_sample_prepared(staged, u, 2).states)
+    node0 = 0
+    for t, plan in enumerate(plans):
+        n = plan.num_nodes
+        dense = np.ones((n, K), dtype=np.float32)
+        dense[0] = root
+        dense[observed[t]] = dense[observed[t]] * emission[obs[t]]
+        weight, states = bridge.maximum(plan, K, dense.ravel(), edges[t], np.float32,
+                                        bridge.MATH_PORTABLE)
+        assert map_weights[t] == weight
+        assert np.array_equal(map_states[node0:node0 + n], states)
+        draw = bridge.sample(plan, K, dense.ravel(), edges[t], uniforms[t], np.float32,
+                             bridge.MATH_PORTABLE)
+        assert np.array_equal(sample_states[node0:node0 + n], draw)
+        node0 += n

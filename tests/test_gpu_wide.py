@@ -1,0 +1,148 @@
+"""Wide state counts (32 < K <= 128): the tensor-core sum-product engine.
+
+Compress products and their adjoints run on tcgen05 in 3xTF32 with FP32
+accumulation; everything else is FP32 with exact power-of-two scaling.
+Tolerances against the FP64 oracle:
+  * log Z: relative error <= 1e-6 for K <= 64 (the narrow FP32 engine's bar);
+    <= 3e-6 for 64 < K <= 128, where every compressed-path entry is an FP32
+    sum of up to 128 products and compress-heavy chains compound it (measured
+    worst 1.7e-6 on a 41-node chain at K = 128);
+  * node and edge marginals: absolute error <= 1e-5 (measured <= 4e-7).
+"""
+import concurrent.futures
+
+import numpy as np
+import pytest
+
+from oracle import bridge
+from parallel_tree_hmm_gb300 import synthetic
+
+pytestmark = pytest.mark.gpu
+
+MARGINAL_ATOL = 1e-5
+
+
+def log_z_rtol(K):
+    return 1e-6 if K <= 64 else 3e-6
+
+
+def shapes(rng, scale):
+    return {
+        "root_only": np.array([-1]),
+        "pair": np.array([-1, 0]),
+        "chain": np.arange(-1, 40),
+        "star": np.array([-1] + [0] * 17),
+        "recursive": synthetic.random_recursive(rng, 3 * scale),
+        "caterpillar": synthetic.caterpillar(2 * scale),
+        "spine_heavy": synthetic.spine_heavy(rng, 3 * scale),
+    }
+
+
+def check_forest(gpu, plans, K, nodes, edges):
+    ws = gpu.Workspace()
+    ws.reserve_forest(plans, K, kind="marginals", scalar=np.float32)
+    view = ws.posterior_marginals_prepared(
+        gpu.BatchedModelView(None, K, len(plans), nodes, edges))
+    log_z = np.array(view.log_partitions, dtype=np.float64)
+    got_nodes = np.array(view.nodes, dtype=np.float64)
+    got_edges = np.array(view.edges, dtype=np.float64)
+    raw = ws.log_partition_function_prepared(
+        gpu.BatchedModelView(None, K, len(plans), nodes, edges))
+    assert np.array_equal(np.array(raw.values), log_z.astype(np.float32))
+
+    offsets = np.cumsum([0] + [p.num_nodes for p in plans])
+    edge_offsets = np.cumsum([0] + [p.num_edges for p in plans])
+
+    def expected(t):
+        n0, n1 = offsets[t], offsets[t + 1]
+        e0, e1 = edge_offsets[t], edge_offsets[t + 1]
+        return bridge.marginals(plans[t], K,
+                                nodes[n0 * K:n1 * K].astype(np.float64),
+                                edges[e0 * K * K:e1 * K * K].astype(np.float64))
+
+    with concurrent.futures.ThreadPoolExecutor(max_workers=16) as pool:
+        results = list(pool.map(expected, range(len(plans))))
+    worst = [0.0, 0.0, 0.0]
+    for t, (z, _, node_m, edge_m) in enumerate(results):
+        n0, n1 = offsets[t], offsets[t + 1]
+        e0, e1 = edge_offsets[t], edge_offsets[t + 1]
+        print(f"  tree {t} ({plans[t].num_nodes} nodes): log Z {z:.6f} "
+              f"rel {abs(log_z[t] - z) / max(1.0, abs(z)):.2e}")
+        worst[0] = max(worst[0], abs(log_z[t] - z) / max(1.0, abs(z)))
+        worst[1] = max(worst[1], np.max(np.abs(got_nodes[n0 * K:n1 * K] - node_m)))
+        worst[2] = max(worst[2], np.max(np.abs(got_edges[e0 * K * K:e1 * K * K] - edge_m),
+                                        initial=0.0))
+    print(f"K={K}: log Z rel {worst[0]:.2e}, node {worst[1]:.2e}, edge {worst[2]:.2e}")
+    assert worst[0] <= log_z_rtol(K)
+    assert worst[1] <= MARGINAL_ATOL
+    assert worst[2] <= MARGINAL_ATOL
+
+
+@pytest.mark.parametrize("K", [33, 64, 100, 128])
+def test_wide_marginals_against_fp64_oracle(gpu, K):
+    rng = np.random.default_rng(900 + K)
+    scale = 100 if K <= 64 else 40
+    plans = [gpu.Plan(p) for p in shapes(rng, scale).values()]
+    node_total = sum(p.num_nodes for p in plans)
+    edge_total = sum(p.num_edges for p in plans)
+    nodes = (rng.random(node_total * K) * 0.9 + 0.1).astype(np.float32)
+    edges = synthetic.stochastic_edges(rng, edge_total, K, 0.5).astype(np.float32)
+    check_forest(gpu, plans, K, nodes, edges)
+
+
+def test_wide_lognormal_factors_with_zeros(gpu):
+    """Dense-contraction workload shapes: spine-heavy trees, K = 64, edge
+    factors lognormal(0, 2) with 5% exact zeros."""
+    rng = np.random.default_rng(64)
+    K = 64
+    plans = [gpu.Plan(synthetic.spine_heavy(rng, n)) for n in (250, 400)]
+    node_total = sum(p.num_nodes for p in plans)
+    edge_total = sum(p.num_edges for p in plans)
+    nodes = synthetic.lognormal(rng, node_total * K, 1.0).astype(np.float32)
+    edges = synthetic.lognormal(rng, edge_total * K * K, 2.0,
+                                zero_fraction=0.05).astype(np.float32)
+    check_forest(gpu, plans, K, nodes, edges)
+
+
+def test_wide_batch_and_categorical_api(gpu):
+    rng = np.random.default_rng(65)
+    K, batch, categories = 48, 3, 5
+    parents = synthetic.random_recursive(rng, 120)
+    plan = gpu.Plan(parents)
+    observed = synthetic.leaves(parents)
+    ws = gpu.Workspace()
+    ws.reserve_categorical_marginals(plan, K, batch, categories, observed,
+                                     scalar=np.float32)
+    staged = ws.categorical_inputs(batch)
+    staged.observations[:] = rng.integers(0, categories, staged.observations.size)
+    staged.root_potential[:] = rng.random(K) + 0.1
+    staged.emission_potentials[:] = rng.random(categories * K) + 0.05
+    staged.edge_potentials[:] = synthetic.stochastic_edges(rng, plan.num_edges, K, 0.5)
+    view = ws.posterior_marginals_prepared(staged, gpu.CategoricalInputUpdate.kAll)
+    obs = staged.observations.reshape(batch, -1)
+    emission = staged.emission_potentials.reshape(categories, K)
+    for b in range(batch):
+        dense = np.ones((plan.num_nodes, K), dtype=np.float32)
+        dense[plan.root] = staged.root_potential
+        dense[observed] = dense[observed] * emission[obs[b]]
+        log_z, _, node_m, edge_m = bridge.marginals(
+            plan, K, dense.astype(np.float64).ravel(),
+            staged.edge_potentials.astype(np.float64))
+        assert abs(view.log_partitions[b] - log_z) <= log_z_rtol(K) * max(1, abs(log_z))
+        assert np.max(np.abs(view.nodes.reshape(batch, -1)[b] - node_m)) <= MARGINAL_ATOL
+        assert np.max(np.abs(view.edges.reshape(batch, -1)[b] - edge_m)) <= MARGINAL_ATOL
+
+
+def test_wide_limits(gpu):
+    plan = gpu.Plan([-1, 0, 0])
+    ws = gpu.Workspace()
+    with pytest.raises(gpu.InvalidArgument):
+        ws.reserve_marginals(plan, 129, 1, scalar=np.float32)
+    with pytest.raises(gpu.InvalidArgument):
+        ws.reserve_maximum(plan, 64, 1, scalar=np.float32)
+    with pytest.raises(gpu.InvalidArgument):
+        ws.reserve_sampling(plan, 40, 1, scalar=np.float32)
+    with pytest.raises(gpu.InvalidArgument):
+        ws.reserve_marginals(plan, 64, 1, scalar=np.float64)
+    with pytest.raises(gpu.InvalidArgument):
+        ws.reserve_marginals(plan, 64, 1, scalar=np.float32, compute=np.float64)
