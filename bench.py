@@ -60,15 +60,25 @@ def parse_args():
     parser.add_argument("--seed", type=int, default=0)
     parser.add_argument("--e2e-steps", type=int, default=None)
     parser.add_argument("--cpu-sample-nodes", type=int, default=20_000_000)
-    parser.add_argument("--workload", choices=["forest", "gw"], default="forest",
+    parser.add_argument("--workload", choices=["forest", "gw", "dense"], default="forest",
                         help="forest: uneven forest, marginals (default); gw: "
-                             "Galton-Watson forest, MAP + posterior sampling")
+                             "Galton-Watson forest, MAP + posterior sampling; dense: "
+                             "spine-heavy trees, K = 64 or 128, tensor-core marginals")
+    parser.add_argument("--tree-nodes", type=int, default=None,
+                        help="dense workload: nodes per tree")
     args = parser.parse_args()
     if args.workload == "gw":
         if args.trees == 4096:
             args.trees = 1024
         if args.states == 4:
             args.states = 8
+    if args.workload == "dense":
+        if args.trees == 4096:
+            args.trees = 256
+        if args.states == 4:
+            args.states = 64
+        if args.tree_nodes is None:
+            args.tree_nodes = 2000 if args.states <= 64 else 500
     return args
 
 
@@ -242,6 +252,8 @@ def main():
 
     if args.workload == "gw":
         run_gw(args, rank, world, local_rank, dist)
+    elif args.workload == "dense":
+        run_dense(args, rank, world, local_rank, dist)
     elif args.impl == "reference":
         run_reference(args, rank, world, dist)
     else:
@@ -666,6 +678,169 @@ def run_gw(args, rank, world, local_rank, dist):
         "gpu_launches": 2 * args.steps,
         "clocks": sampler.summary(),
     }
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+
+
+# -------------------------------------------- dense-contraction workload
+def run_dense(args, rank, world, local_rank, dist):
+    """Spine-heavy random recursive trees (node i attaches to i - 1 with
+    probability 0.95, else to a uniform earlier node), K = 64 or 128, dense
+    node factors lognormal(0, 1), edge factors lognormal(0, 2) with 5% exact
+    zeros; log Z and all marginals on the tensor-core engine. The trees are
+    scaled down from 100,000 nodes so that the edge factors fit in HBM and
+    host memory (--tree-nodes)."""
+    import parallel_tree_hmm_gb300 as thmm
+    from oracle import bridge
+    from parallel_tree_hmm_gb300 import synthetic
+
+    K = args.states
+    rng = np.random.default_rng(rank_seed(args.seed, rank))
+    parents = [synthetic.spine_heavy(rng, args.tree_nodes) for _ in range(args.trees)]
+    plans = [thmm.Plan(p) for p in parents]
+    total_nodes = sum(p.num_nodes for p in plans)
+    total_edges = sum(p.num_edges for p in plans)
+    compressions = sum(int(p.num_compressions) for p in plans)
+    config = {
+        "workload": (f"dense contractions: {args.trees} spine-heavy trees of {args.tree_nodes} "
+                     f"nodes (spine probability 0.95), K={K}, lognormal(0,1) node and "
+                     f"lognormal(0,2) edge factors with 5% zeros, marginals"),
+        "trees": args.trees, "nodes_per_rank": total_nodes, "states": K,
+        "compressions_per_rank": compressions, "seed": args.seed,
+        "parallelism": f"replicas per GPU x{args.gpus}",
+        "l2": "inputs larger than L2 (edge factors of one step > 129 MB)",
+        "scaled_from": "256 trees x 100,000 nodes (1.7 TB of edge factors at K=128)",
+    }
+    metric = "tree-nodes/s for logZ+marginals+grad (dense contractions)"
+
+    def edge_chunks(fill):
+        chunk = 1 << 24
+        values = total_edges * K * K
+        for start in range(0, values, chunk):
+            n = min(chunk, values - start)
+            block = np.exp(2.0 * rng.standard_normal(n, dtype=np.float32))
+            block[rng.random(n, dtype=np.float32) < 0.05] = 0.0
+            fill(start, block)
+
+    node_factors = np.exp(rng.standard_normal(total_nodes * K, dtype=np.float32))
+
+    if args.impl == "reference" or (rank == 0 and world == 1 and args.cpu_sample_nodes > 0):
+        sample = min(16, args.trees)
+        edge0 = np.cumsum([0] + [p.num_edges for p in plans])
+        node0 = np.cumsum([0] + [p.num_nodes for p in plans])
+        sample_edges = np.empty(int(edge0[sample]) * K * K, dtype=np.float32)
+
+        def keep(start, block):
+            stop = min(start + len(block), sample_edges.size)
+            if start < stop:
+                sample_edges[start:stop] = block[:stop - start]
+
+        state = rng.bit_generator.state
+        edge_chunks(keep)
+        rng.bit_generator.state = state
+
+        def job(t):
+            bridge.marginals(plans[t], K,
+                             node_factors[node0[t] * K:node0[t + 1] * K].astype(np.float64),
+                             sample_edges[edge0[t] * K * K:edge0[t + 1] * K * K]
+                             .astype(np.float64))
+            return plans[t].num_nodes
+
+        start = time.perf_counter()
+        with concurrent.futures.ThreadPoolExecutor(os.cpu_count() or 1) as pool:
+            done = sum(pool.map(job, range(sample)))
+        cpu = {"value": done / (time.perf_counter() - start), "unit": UNIT,
+               "cores": os.cpu_count() or 1, "kind": "port",
+               "sample": f"first {sample} trees, FP64 log-domain marginals"}
+        if args.impl == "reference":
+            if rank == 0:
+                print(json.dumps({
+                    "impl": "reference", "metric": metric, "value": cpu["value"],
+                    "unit": UNIT, "n_gpus": args.gpus, "steps": 1, "warmup": 0,
+                    "ms_per_step": None, "higher_is_better": True, "scaling": "weak",
+                    "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+                    "config": config, "cpu_baseline": cpu,
+                    "e2e": {"value": cpu["value"], "unit": UNIT, "h2d_bytes_per_step": 0,
+                            "d2h_bytes_per_step": 0}}), flush=True)
+            return
+    else:
+        cpu = None
+
+    import torch
+
+    device = local_rank
+    torch.cuda.set_device(device)
+    ws = thmm.Workspace()
+    ws.reserve_forest(plans, K, device, kind="marginals", scalar=np.float32)
+    staged = ws.inputs()
+    staged.node_potentials[:] = node_factors
+
+    def fill(start, block):
+        staged.edge_potentials[start:start + len(block)] = block
+
+    edge_chunks(fill)
+    first = ws.posterior_marginals_prepared(staged)
+    finite = bool(np.all(np.isfinite(first.log_partitions)))
+    node_sum_error = float(np.max(np.abs(
+        np.array(first.nodes).reshape(-1, K).sum(axis=1) - 1.0)))
+
+    ext = torch.cuda.ExternalStream(ws.stream, device=device)
+    for _ in range(args.warmup):
+        ws.enqueue(4)
+    torch.cuda.synchronize(device)
+    if dist is not None:
+        dist.barrier()
+    sampler = ClockSampler(device)
+    with sampler:
+        begin = torch.cuda.Event(enable_timing=True)
+        end = torch.cuda.Event(enable_timing=True)
+        begin.record(ext)
+        for _ in range(args.steps):
+            ws.enqueue(4)
+        end.record(ext)
+        end.synchronize()
+    step_ms = reduce_max(begin.elapsed_time(end), dist) / args.steps
+    value = total_nodes * world / (step_ms / 1e3)
+
+    e2e_steps = args.e2e_steps or 3
+    e2e_total = 0.0
+    for _ in range(e2e_steps):
+        torch.cuda.synchronize(device)
+        t0 = time.perf_counter()
+        ws.posterior_marginals_prepared(staged)
+        e2e_total += time.perf_counter() - t0
+    e2e_total = reduce_max(e2e_total, dist)
+
+    S = 4
+    algorithmic = (2 * total_edges * K * K * S + 2 * total_nodes * K * S + len(plans) * S)
+    # Useful tensor-core work: 2 K^3 per product, one product per compression
+    # forward and three in the adjoint.
+    useful_flops = 4 * 2 * compressions * K ** 3
+    peaks = json.loads((ROOT / "MEASURED_PEAKS.json").read_text()) \
+        if (ROOT / "MEASURED_PEAKS.json").exists() else {}
+    peak = peaks.get("hbm_gbs", 6800.0)
+    achieved = algorithmic / (step_ms / 1e3) / 1e9
+    line = {
+        "metric": metric, "value": value, "unit": UNIT, "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": step_ms,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32 (3xTF32 tensor-core products)", "data": "synthetic",
+        "config": {**config, "all_log_z_finite": finite,
+                   "node_marginal_normalisation_error": node_sum_error,
+                   "useful_tensor_tflops": useful_flops / (step_ms / 1e3) / 1e12},
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                     "frac": achieved / peak,
+                     "peak_source": "measured" if peaks else "fallback",
+                     "traffic": None, "algorithmic_bytes_per_launch": algorithmic},
+        "e2e": {"value": total_nodes * world * e2e_steps / e2e_total, "unit": UNIT,
+                "h2d_bytes_per_step": (total_edges * K * K + total_nodes * K) * S,
+                "d2h_bytes_per_step": (total_edges * K * K + total_nodes * K) * S
+                + len(plans) * S + 16},
+        "gpu_launches": 2 * args.steps,
+        "clocks": sampler.summary(),
+    }
+    if cpu is not None:
+        line["cpu_baseline"] = cpu
     if rank == 0:
         print(json.dumps(line), flush=True)
 
