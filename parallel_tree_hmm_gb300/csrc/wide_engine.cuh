@@ -25,6 +25,7 @@
 #define THMM_WIDE_ENGINE_CUH_
 
 #include <cstdint>
+#include <type_traits>
 #include <cuda_runtime.h>
 
 #include "engine.cuh"
@@ -89,17 +90,104 @@ __device__ __forceinline__ float BlockMax(float v, Shared &sh) {
   return m;
 }
 
+// Operand sources. A product operand is a K x K block of a row-major K x K
+// matrix in global memory, read either as stored (element (r, d) at
+// p[r * K + d], optionally times scale[d]) or transposed (element (r, d) at
+// p[d * K + r]).
+struct RowMajor {
+  const float *p;
+  const float *scale; // shared-memory column scale, or null
+  __device__ __forceinline__ float operator()(unsigned K, unsigned r, unsigned d) const {
+    const float v = p[static_cast<std::size_t>(r) * K + d];
+    return scale != nullptr ? v * scale[d] : v;
+  }
+  // Elements d .. d + 3 of row r (K a multiple of 4, so 16-byte aligned).
+  __device__ __forceinline__ float4 Quad(unsigned K, unsigned r, unsigned d) const {
+    float4 v = *reinterpret_cast<const float4 *>(p + static_cast<std::size_t>(r) * K + d);
+    if (scale != nullptr) {
+      v.x *= scale[d];
+      v.y *= scale[d + 1];
+      v.z *= scale[d + 2];
+      v.w *= scale[d + 3];
+    }
+    return v;
+  }
+};
+struct Transposed {
+  const float *p;
+  __device__ __forceinline__ float operator()(unsigned K, unsigned r, unsigned d) const {
+    return p[static_cast<std::size_t>(d) * K + r];
+  }
+};
+
+__device__ __forceinline__ void StoreSplit(unsigned char *hi, unsigned char *lo,
+                                           std::uint32_t at, float v) {
+  const float h = Hi(v);
+  *reinterpret_cast<float *>(hi + at) = h;
+  *reinterpret_cast<float *>(lo + at) = v - h;
+}
+__device__ __forceinline__ void StoreSplit(unsigned char *hi, unsigned char *lo,
+                                           std::uint32_t at, float4 v) {
+  const float4 h = make_float4(Hi(v.x), Hi(v.y), Hi(v.z), Hi(v.w));
+  *reinterpret_cast<float4 *>(hi + at) = h;
+  *reinterpret_cast<float4 *>(lo + at) = make_float4(v.x - h.x, v.y - h.y, v.z - h.z, v.w - h.w);
+}
+
+// Writes rows r < K, depths [d0, d0 + kChunk) ∩ [0, K) of one operand as
+// TF32 hi/lo parts; everything else in the buffers stays zero (they are
+// cleared once per launch), so padded rows and depths contribute nothing.
+template <class Source>
+__device__ __forceinline__ void Stage(const Source &src, unsigned K, unsigned d0,
+                                      unsigned char *hi, unsigned char *lo) {
+  const unsigned depth = K > d0 ? (K - d0 < kChunk ? K - d0 : kChunk) : 0u;
+  if (d0 != 0 && depth < kChunk) {
+    // A later chunk: clear depths [depth, kChunk) left over from the first.
+    const unsigned pad = kChunk - depth;
+    for (unsigned idx = threadIdx.x; idx < K * pad; idx += kThreads) {
+      const std::uint32_t at = umma::CoreOffset(idx / pad, depth + idx % pad, kSbo);
+      *reinterpret_cast<float *>(hi + at) = 0.0f;
+      *reinterpret_cast<float *>(lo + at) = 0.0f;
+    }
+  }
+  if constexpr (std::is_same_v<Source, RowMajor>) {
+    if (K % 4 == 0) {
+      const unsigned quads = depth / 4;
+#pragma unroll 4
+      for (unsigned idx = threadIdx.x; idx < K * quads; idx += kThreads) {
+        const unsigned r = idx / quads, q = idx % quads;
+        StoreSplit(hi, lo, umma::CoreOffset(r, 4 * q, kSbo), src.Quad(K, r, d0 + 4 * q));
+      }
+      return;
+    }
+#pragma unroll 4
+    for (unsigned idx = threadIdx.x; idx < K * depth; idx += kThreads) {
+      const unsigned r = idx / depth, d = idx % depth;
+      StoreSplit(hi, lo, umma::CoreOffset(r, d, kSbo), src(K, r, d0 + d));
+    }
+  } else {
+#pragma unroll 4
+    for (unsigned idx = threadIdx.x; idx < K * depth; idx += kThreads) {
+      const unsigned r = idx % K, d = idx / K;
+      StoreSplit(hi, lo, umma::CoreOffset(r, d, kSbo), src(K, r, d0 + d));
+    }
+  }
+}
+
+// Clears the four operand buffers (once per launch).
+__device__ __forceinline__ void ClearOperands(unsigned char *smem) {
+  float4 *p = reinterpret_cast<float4 *>(smem);
+  for (unsigned i = threadIdx.x; i < 4 * kOperandBytes / 16; i += kThreads)
+    p[i] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+}
+
 // Tensor-memory lanes 0..127 (one per thread), columns [column, column + KP):
-//   D[r][n] = sum_d X(r, d) * Y(n, d),  r < 128, n < KP, d < KP,
-// in 3xTF32 with FP32 accumulation. The functors return 0 outside the K x K
-// block. kXRows (kYRows): the source of X (Y) is read with d running fastest
-// across threads (row-major source); otherwise r (n) runs fastest. Returns
-// false if a tensor-core wait timed out.
-template <int KP, bool kXRows, bool kYRows, class XF, class YF>
+//   D[r][n] = sum_{d < K} X(r, d) * Y(n, d)
+// for r, n < K (other lanes and columns hold values nobody reads), in 3xTF32
+// with FP32 accumulation. Returns false if a tensor-core wait timed out.
+template <int KP, class XS, class YS>
 __device__ bool Product(unsigned char *smem, Shared &sh, std::uint32_t &phase,
-                        std::uint32_t tmem, XF x, YF y) {
+                        std::uint32_t tmem, unsigned K, const XS &x, const YS &y) {
   static_assert(KP % kChunk == 0 && KP <= 128, "padded state count");
-  const unsigned tid = threadIdx.x;
   unsigned char *const xh = smem;
   unsigned char *const xl = smem + kOperandBytes;
   unsigned char *const yh = smem + 2 * kOperandBytes;
@@ -109,31 +197,13 @@ __device__ bool Product(unsigned char *smem, Shared &sh, std::uint32_t &phase,
 #pragma unroll 1
   for (unsigned chunk = 0; chunk < KP / kChunk; ++chunk) {
     const unsigned d0 = chunk * kChunk;
-#pragma unroll 4
-    for (unsigned idx = tid; idx < 128 * kChunk; idx += kThreads) {
-      const unsigned r = kXRows ? idx / kChunk : idx % 128;
-      const unsigned d = kXRows ? idx % kChunk : idx / 128;
-      const float v = x(r, d0 + d);
-      const float h = Hi(v);
-      const std::uint32_t at = umma::CoreOffset(r, d, kSbo);
-      *reinterpret_cast<float *>(xh + at) = h;
-      *reinterpret_cast<float *>(xl + at) = v - h;
-    }
-#pragma unroll 4
-    for (unsigned idx = tid; idx < KP * kChunk; idx += kThreads) {
-      const unsigned n = kYRows ? idx / kChunk : idx % KP;
-      const unsigned d = kYRows ? idx % kChunk : idx / KP;
-      const float v = y(n, d0 + d);
-      const float h = Hi(v);
-      const std::uint32_t at = umma::CoreOffset(n, d, kSbo);
-      *reinterpret_cast<float *>(yh + at) = h;
-      *reinterpret_cast<float *>(yl + at) = v - h;
-    }
+    Stage(x, K, d0, xh, xl);
+    Stage(y, K, d0, yh, yl);
     umma::FenceOperands();
     umma::FenceBeforeSync();
     __syncthreads();
     umma::FenceAfterSync();
-    if (tid == 0) {
+    if (threadIdx.x == 0) {
       const std::uint32_t xh_at = umma::SmemAddress(xh), xl_at = umma::SmemAddress(xl);
       const std::uint32_t yh_at = umma::SmemAddress(yh), yl_at = umma::SmemAddress(yl);
       const std::uint32_t a_parts[3] = {xl_at, xh_at, xh_at};

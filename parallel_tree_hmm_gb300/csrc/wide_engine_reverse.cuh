@@ -36,19 +36,43 @@ template <int KP> __device__ void Tree<KP>::Reverse() {
         if (j < K)
           ratio[j] = msg[j] > 0.0f ? v[j] / msg[j] : 0.0f;
         __syncthreads();
-        // Path adjoint rows: ratio[r] * path[r][c] * leaf[c] (coalesced rows).
+        // Path adjoint rows ratio[r] * path[r][c] * leaf[c] (warp w: rows
+        // w, w + 4, ...; lanes: columns, coalesced), and each warp's partial
+        // column sums sum_r ratio[r] * path[r][c] for the leaf adjoint.
         float *out = adjoint_of(op.x);
-        for (unsigned r = warp; r < K; r += kThreads / 32)
-          for (unsigned c = lane; c < K; c += 32)
-            out[static_cast<std::size_t>(r) * K + c] =
-                ratio[r] * path[static_cast<std::size_t>(r) * K + c] * leaf[c];
-        // Leaf adjoint: leaf[c] * sum_r ratio[r] * path[r][c].
-        if (j < K) {
-          float column = 0.0f;
-          for (unsigned r = 0; r < K; ++r)
-            column = fmaf(ratio[r], path[static_cast<std::size_t>(r) * K + j], column);
-          node_out[static_cast<std::size_t>(op.y & kMask) * K + j] = leaf[j] * column;
+        float column[KP / 32];
+#pragma unroll
+        for (unsigned q = 0; q < KP / 32; ++q)
+          column[q] = 0.0f;
+#pragma unroll 2
+        for (unsigned r = warp; r < K; r += kThreads / 32) {
+          const float ratio_r = ratio[r];
+#pragma unroll
+          for (unsigned q = 0; q < KP / 32; ++q) {
+            const unsigned c = lane + 32 * q;
+            if (c < K) {
+              const float p = path[static_cast<std::size_t>(r) * K + c];
+              out[static_cast<std::size_t>(r) * K + c] = ratio_r * p * leaf[c];
+              column[q] = fmaf(ratio_r, p, column[q]);
+            }
+          }
         }
+        // Reduce the four warps' column sums through the message vector.
+#pragma unroll 1
+        for (unsigned w = 0; w < kThreads / 32; ++w) {
+          if (warp == w) {
+#pragma unroll
+            for (unsigned q = 0; q < KP / 32; ++q) {
+              const unsigned c = lane + 32 * q;
+              if (c < K)
+                msg[c] = (w == 0 ? 0.0f : msg[c]) + column[q];
+            }
+          }
+          __syncthreads();
+        }
+        // Leaf adjoint: leaf[c] * sum_r ratio[r] * path[r][c].
+        if (j < K)
+          node_out[static_cast<std::size_t>(op.y & kMask) * K + j] = leaf[j] * msg[j];
         __syncthreads();
       }
     } else if (step.kind == kStepCompress) {
@@ -61,17 +85,10 @@ template <int KP> __device__ void Tree<KP>::Reverse() {
         float *output_adjoint = comp_mu + static_cast<std::size_t>(tape) * KK;
         NodeVector(op.y, op.w, middle);
         __syncthreads();
-        const unsigned K_ = K;
         const float *mid = middle;
         // Unnormalised output, recomputed: left * diag(middle) * right.
-        ok = Product<KP, true, false>(
-                 smem, sh, phase, tmem + kProductColumn,
-                 [=](unsigned r, unsigned d) {
-                   return r < K_ && d < K_ ? left[r * K_ + d] * mid[d] : 0.0f;
-                 },
-                 [=](unsigned n, unsigned d) {
-                   return n < K_ && d < K_ ? right[d * K_ + n] : 0.0f;
-                 }) &&
+        ok = Product<KP>(smem, sh, phase, tmem + kProductColumn, K,
+                         RowMajor{left, middle}, Transposed{right}) &&
              ok;
         // ratio = adjoint / output, written over the output adjoint (each
         // path version's adjoint is read only here).
@@ -96,24 +113,12 @@ template <int KP> __device__ void Tree<KP>::Reverse() {
         __syncthreads();
         const float *ratio_matrix = output_adjoint;
         // P1[r][m] = sum_c ratio[r][c] right[m][c]  (left adjoint factor).
-        ok = Product<KP, true, true>(
-                 smem, sh, phase, tmem + kLeftColumn,
-                 [=](unsigned r, unsigned c) {
-                   return r < K_ && c < K_ ? ratio_matrix[r * K_ + c] : 0.0f;
-                 },
-                 [=](unsigned m, unsigned c) {
-                   return m < K_ && c < K_ ? right[m * K_ + c] : 0.0f;
-                 }) &&
+        ok = Product<KP>(smem, sh, phase, tmem + kLeftColumn, K,
+                         RowMajor{ratio_matrix, nullptr}, RowMajor{right, nullptr}) &&
              ok;
         // P2[m][c] = sum_r left[r][m] ratio[r][c]  (right adjoint factor).
-        ok = Product<KP, false, false>(
-                 smem, sh, phase, tmem + kRightColumn,
-                 [=](unsigned m, unsigned r) {
-                   return m < K_ && r < K_ ? left[r * K_ + m] : 0.0f;
-                 },
-                 [=](unsigned c, unsigned r) {
-                   return c < K_ && r < K_ ? ratio_matrix[r * K_ + c] : 0.0f;
-                 }) &&
+        ok = Product<KP>(smem, sh, phase, tmem + kRightColumn, K, Transposed{left},
+                         Transposed{ratio_matrix}) &&
              ok;
         // Row j: left adjoint left[j][m] middle[m] P1[j][m]; right adjoint
         // right[j][c] middle[j] P2[j][c]; middle adjoint sum_c of the latter.
@@ -155,6 +160,7 @@ template <int KP, int kPart>
 __global__ void __launch_bounds__(kThreads, 1) WideKernel(EngineArgs args) {
   extern __shared__ __align__(1024) unsigned char dynamic_smem[];
   __shared__ Shared sh;
+  ClearOperands(dynamic_smem);
   if (threadIdx.x == 0)
     umma::BarrierInit(&sh.barrier);
   if (threadIdx.x < 32)

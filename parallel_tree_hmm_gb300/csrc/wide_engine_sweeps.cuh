@@ -49,19 +49,9 @@ template <int KP> __device__ void Tree<KP>::Forward() {
         const uint4 op = compress[g];
         NodeVector(op.y, op.w, middle);
         __syncthreads();
-        const float *left = Path(op.x);
-        const float *right = Path(op.z);
-        const unsigned K_ = K;
-        const float *mid = middle;
         // X(r, d) = left[r][d] * middle[d]; Y(n, d) = right[d][n].
-        ok = Product<KP, true, false>(
-                 smem, sh, phase, tmem + kProductColumn,
-                 [=](unsigned r, unsigned d) {
-                   return r < K_ && d < K_ ? left[r * K_ + d] * mid[d] : 0.0f;
-                 },
-                 [=](unsigned n, unsigned d) {
-                   return n < K_ && d < K_ ? right[d * K_ + n] : 0.0f;
-                 }) &&
+        ok = Product<KP>(smem, sh, phase, tmem + kProductColumn, K,
+                         RowMajor{Path(op.x), middle}, Transposed{Path(op.z)}) &&
              ok;
         // Row j of the product is tensor-memory lane j: maximum, then scale.
         const std::uint32_t lane_base =
