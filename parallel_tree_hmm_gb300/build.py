@@ -31,15 +31,36 @@ COMMON = [
     f"-I{CSRC}",
 ]
 SOURCES = [
-    "btrc_plan.cc",
-    "program.cc",
-    "runtime.cc",
-    "engine_linear_f32.cu",
+    # Slowest first: the build compiles them in parallel.
+    "engine_linear_fd_rev_large.cu",
+    "engine_linear_dd_rev_large.cu",
+    "engine_linear_ff_rev_large.cu",
+    "engine_linear_df_rev_large.cu",
+    "engine_linear_fd_fwd_large.cu",
+    "engine_linear_dd_fwd_large.cu",
+    "engine_linear_ff_fwd_large.cu",
+    "engine_linear_df_fwd_large.cu",
+    "engine_linear_fd_rev_small.cu",
+    "engine_linear_dd_rev_small.cu",
+    "engine_linear_ff_rev_small.cu",
+    "engine_linear_df_rev_small.cu",
+    "engine_linear_fd_fwd_small.cu",
+    "engine_linear_dd_fwd_small.cu",
+    "engine_linear_ff_fwd_small.cu",
+    "engine_linear_df_fwd_small.cu",
+    "engine_maximum_f64.cu",
+    "engine_maximum_f32.cu",
+    "engine_sample_f64.cu",
+    "engine_sample_f32.cu",
     "engine_wide.cu",
+    "engine_linear_f32.cu",
     "engine_linear_f64.cu",
     "engine_maximum.cu",
     "engine_sample.cu",
     "static_scratch.cu",
+    "runtime.cc",
+    "program.cc",
+    "btrc_plan.cc",
 ]
 
 

@@ -54,8 +54,11 @@ constexpr int kThreads = THMM_CTA_THREADS;
 constexpr int kWarps = kThreads / 32;
 constexpr unsigned kFull = 0xffffffffu;
 
-// Lanes per operation group for a padded state count.
-template <int KMAX> constexpr int GroupLanes() { return KMAX <= 4 ? 1 : KMAX; }
+// Lanes per operation group for a padded state count: one lane per row, the
+// group a power of two (shuffle width); lanes beyond K hold zero rows.
+template <int KMAX> constexpr int GroupLanes() {
+  return KMAX <= 4 ? 1 : KMAX <= 8 ? 8 : KMAX <= 16 ? 16 : 32;
+}
 
 template <bool kCta> struct Team {
   unsigned tid;
@@ -401,6 +404,8 @@ template <int KMAX, int kPart, bool kWide> constexpr int LinearMinBlocks() {
     return kPart == kLinearForward ? 4 : 2;
   else if constexpr (KMAX <= 8 || (KMAX <= 16 && !kWide))
     return 4;
+  else if constexpr (KMAX <= 24 && !kWide)
+    return 3;
   else
     return 2;
 }
@@ -409,7 +414,7 @@ template <typename Scalar, typename Compute, int KMAX, int kPart = kLinearForwar
 struct LinearEngine {
   static constexpr int kMinBlocks = LinearMinBlocks<KMAX, kPart, sizeof(Compute) == 8>();
   static constexpr int G = GroupLanes<KMAX>();
-  static constexpr int ROWS = KMAX / G;
+  static constexpr int ROWS = (KMAX + G - 1) / G;
   using Ctx = Context<Scalar, Compute, KMAX>;
   Ctx c;
   Compute *comp_mu;
@@ -945,7 +950,7 @@ template <typename T, int KMAX> struct LogContext {
 template <typename T, int KMAX> struct MaxEngine {
   static constexpr int kMinBlocks = KMAX <= 8 ? 4 : 2;
   static constexpr int G = GroupLanes<KMAX>();
-  static constexpr int ROWS = KMAX / G;
+  static constexpr int ROWS = (KMAX + G - 1) / G;
   LogContext<T, KMAX> lc;
   const Context<T, T, KMAX> &c;
   std::uint8_t *rake_choices;
@@ -1188,7 +1193,7 @@ __device__ __forceinline__ unsigned SampleLogWeights(const T (&terms)[KMAX],
 template <typename T, int KMAX> struct SampleEngine {
   static constexpr int kMinBlocks = KMAX <= 8 ? 4 : 2;
   static constexpr int G = GroupLanes<KMAX>();
-  static constexpr int ROWS = KMAX / G;
+  static constexpr int ROWS = (KMAX + G - 1) / G;
   LogContext<T, KMAX> lc;
   const Context<T, T, KMAX> &c;
 

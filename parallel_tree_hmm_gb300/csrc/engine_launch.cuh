@@ -31,37 +31,41 @@ cudaError_t LaunchOrQuery(const EngineArgs &args, int grid, cudaStream_t stream,
   return cudaGetLastError();
 }
 
-template <typename Scalar, typename Compute, int kPart>
-cudaError_t LaunchLinearPart(unsigned kmax, const EngineArgs &args, int grid,
+// Launches (or queries) the sum-product kernel of one part for padded state
+// count kmax, restricted to kmax <= 16 (kSmall) or > 16 so that each half
+// compiles in its own translation unit.
+template <typename Scalar, typename Compute, int kPart, bool kSmall>
+cudaError_t LaunchLinearHalf(unsigned kmax, const EngineArgs &args, int grid,
                              cudaStream_t stream, int *blocks_per_sm) {
-  switch (kmax) {
-  case 4:
-    return LaunchOrQuery<LinearEngine<Scalar, Compute, 4, kPart>, Compute, true>(
-        args, grid, stream, blocks_per_sm);
-  case 8:
-    return LaunchOrQuery<LinearEngine<Scalar, Compute, 8, kPart>, Compute, true>(
-        args, grid, stream, blocks_per_sm);
-  case 16:
-    return LaunchOrQuery<LinearEngine<Scalar, Compute, 16, kPart>, Compute, true>(
-        args, grid, stream, blocks_per_sm);
-  case 32:
-    return LaunchOrQuery<LinearEngine<Scalar, Compute, 32, kPart>, Compute, true>(
-        args, grid, stream, blocks_per_sm);
-  default:
-    return cudaErrorInvalidValue;
+  if constexpr (kSmall) {
+    switch (kmax) {
+    case 4:
+      return LaunchOrQuery<LinearEngine<Scalar, Compute, 4, kPart>, Compute, true>(
+          args, grid, stream, blocks_per_sm);
+    case 8:
+      return LaunchOrQuery<LinearEngine<Scalar, Compute, 8, kPart>, Compute, true>(
+          args, grid, stream, blocks_per_sm);
+    case 16:
+      return LaunchOrQuery<LinearEngine<Scalar, Compute, 16, kPart>, Compute, true>(
+          args, grid, stream, blocks_per_sm);
+    default:
+      return cudaErrorInvalidValue;
+    }
+  } else {
+    switch (kmax) {
+    case 20:
+      return LaunchOrQuery<LinearEngine<Scalar, Compute, 20, kPart>, Compute, true>(
+          args, grid, stream, blocks_per_sm);
+    case 24:
+      return LaunchOrQuery<LinearEngine<Scalar, Compute, 24, kPart>, Compute, true>(
+          args, grid, stream, blocks_per_sm);
+    case 32:
+      return LaunchOrQuery<LinearEngine<Scalar, Compute, 32, kPart>, Compute, true>(
+          args, grid, stream, blocks_per_sm);
+    default:
+      return cudaErrorInvalidValue;
+    }
   }
-}
-
-// `part` selects the forward sweep (kLinearForward) or the adjoint sweep
-// (kLinearReverse).
-template <typename Scalar, typename Compute>
-cudaError_t LaunchLinearTyped(unsigned kmax, int part, const EngineArgs &args, int grid,
-                              cudaStream_t stream, int *blocks_per_sm) {
-  return part == kLinearReverse
-             ? LaunchLinearPart<Scalar, Compute, kLinearReverse>(kmax, args, grid, stream,
-                                                                 blocks_per_sm)
-             : LaunchLinearPart<Scalar, Compute, kLinearForward>(kmax, args, grid, stream,
-                                                                 blocks_per_sm);
 }
 
 template <template <typename, int> class Engine, typename T>
@@ -74,6 +78,10 @@ cudaError_t LaunchLogTyped(unsigned kmax, const EngineArgs &args, int grid,
     return LaunchOrQuery<Engine<T, 8>, T, false>(args, grid, stream, blocks_per_sm);
   case 16:
     return LaunchOrQuery<Engine<T, 16>, T, false>(args, grid, stream, blocks_per_sm);
+  case 20:
+    return LaunchOrQuery<Engine<T, 20>, T, false>(args, grid, stream, blocks_per_sm);
+  case 24:
+    return LaunchOrQuery<Engine<T, 24>, T, false>(args, grid, stream, blocks_per_sm);
   case 32:
     return LaunchOrQuery<Engine<T, 32>, T, false>(args, grid, stream, blocks_per_sm);
   default:

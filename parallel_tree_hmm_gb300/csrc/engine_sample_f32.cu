@@ -1,0 +1,12 @@
+// Posterior-sampling kernels, float arithmetic (one translation unit per
+// instance so the build compiles them in parallel).
+#include "engine_launch.cuh"
+
+namespace thmm {
+
+cudaError_t LaunchSampleF32(unsigned kmax, const EngineArgs &args, int grid, cudaStream_t stream,
+                 int *blocks_per_sm) {
+  return LaunchLogTyped<SampleEngine, float>(kmax, args, grid, stream, blocks_per_sm);
+}
+
+} // namespace thmm

@@ -39,7 +39,8 @@ struct ProgramSet {
                     bool categorical);
 };
 
-// Kernel entry points. `kmax` is the padded state count (4, 8, 16 or 32).
+// Kernel entry points. `kmax` is the padded state count (4, 8, 16, 20, 24
+// or 32; 64 or 128 for the wide-state engine).
 // With `blocks_per_sm` non-null the call only reports the occupancy. The
 // linear (sum-product) kernels come in two parts: 0 = forward sweep (log Z,
 // root marginal), 1 = adjoint sweep (marginals), launched in that order.
@@ -55,6 +56,29 @@ cudaError_t LaunchMaximum(int scalar_bytes, unsigned kmax,
 cudaError_t LaunchSample(int scalar_bytes, unsigned kmax, const EngineArgs &args,
                          int grid, cudaStream_t stream, int *blocks_per_sm);
 
+// Per-instance launchers behind the dispatchers above, one translation unit
+// each (engine_linear_<scalar><compute>_<part>_<half>.cu for padded state
+// counts up to 16 (Small) or above (Large), engine_maximum_f*.cu,
+// engine_sample_f*.cu) so that the build compiles them in parallel.
+#define THMM_DECLARE_LAUNCHER(NAME)                                                  \
+  cudaError_t NAME(unsigned kmax, const EngineArgs &args, int grid, cudaStream_t stream, \
+                   int *blocks_per_sm);
+#define THMM_DECLARE_LINEAR(TYPES)                                                   \
+  THMM_DECLARE_LAUNCHER(LaunchLinear##TYPES##ForwardSmall)                            \
+  THMM_DECLARE_LAUNCHER(LaunchLinear##TYPES##ForwardLarge)                            \
+  THMM_DECLARE_LAUNCHER(LaunchLinear##TYPES##ReverseSmall)                            \
+  THMM_DECLARE_LAUNCHER(LaunchLinear##TYPES##ReverseLarge)
+THMM_DECLARE_LINEAR(FF)
+THMM_DECLARE_LINEAR(FD)
+THMM_DECLARE_LINEAR(DF)
+THMM_DECLARE_LINEAR(DD)
+THMM_DECLARE_LAUNCHER(LaunchMaximumF32)
+THMM_DECLARE_LAUNCHER(LaunchMaximumF64)
+THMM_DECLARE_LAUNCHER(LaunchSampleF32)
+THMM_DECLARE_LAUNCHER(LaunchSampleF64)
+#undef THMM_DECLARE_LINEAR
+#undef THMM_DECLARE_LAUNCHER
+
 // Tensor-core sum-product kernels for 32 < K <= 128 (kmax 64 or 128, FP32).
 cudaError_t LaunchWide(unsigned kmax, int part, const EngineArgs &args, int grid,
                        cudaStream_t stream, int *blocks_per_sm);
@@ -63,6 +87,8 @@ inline unsigned PaddedStates(std::size_t states) {
   return states <= 4    ? 4u
          : states <= 8  ? 8u
          : states <= 16 ? 16u
+         : states <= 20 ? 20u
+         : states <= 24 ? 24u
          : states <= 32 ? 32u
          : states <= 64 ? 64u
                         : 128u;

@@ -27,7 +27,8 @@
 #include <stdexcept>
 #include <string>
 
-#include "engine_launch.cuh"
+#include "engine.cuh" // kWarps (CTA shape shared with the engine kernels)
+#include "program.h"
 #include "program_builder.h"
 #include "thmm_gb300.h"
 
@@ -49,7 +50,7 @@ struct DeviceSetup {
   bool ready = false;
   unsigned char *scratch = nullptr;
   int sms = 0;
-  int occupancy[4] = {0, 0, 0, 0}; // per padded state count 4, 8, 16, 32
+  int occupancy[6] = {0, 0, 0, 0, 0, 0}; // per padded state count 4, 8, 16, 20, 24, 32
 };
 DeviceSetup g_devices[kMaxDevices];
 
@@ -138,10 +139,10 @@ DeviceSetup &Setup(int device) {
     setup.scratch = static_cast<unsigned char *>(address);
     Check(cudaDeviceGetAttribute(&setup.sms, cudaDevAttrMultiProcessorCount, device),
           "cudaDeviceGetAttribute");
-    const unsigned kmax[4] = {4, 8, 16, 32};
+    const unsigned kmax[6] = {4, 8, 16, 20, 24, 32};
     EngineArgs probe{};
-    for (int i = 0; i < 4; ++i)
-      Check(LaunchLinearTyped<float, float>(kmax[i], kLinearForward, probe, 0, nullptr,
+    for (int i = 0; i < 6; ++i)
+      Check(LaunchLinearF32(false, kmax[i], kLinearForward, probe, 0, nullptr,
                                             &setup.occupancy[i]),
             "occupancy query");
     setup.ready = true;
@@ -251,12 +252,17 @@ extern "C" thmm_status thmm_log_partition_static(
     args.states = static_cast<std::uint32_t>(states);
     args.scratch = base + image_bytes;
     args.values = log_partitions;
-    const int index = kmax == 4 ? 0 : kmax == 8 ? 1 : kmax == 16 ? 2 : 3;
+    const int index = kmax == 4    ? 0
+                      : kmax == 8  ? 1
+                      : kmax == 16 ? 2
+                      : kmax == 20 ? 3
+                      : kmax == 24 ? 4
+                                   : 5;
     const std::size_t teams = big ? batch : (batch + kWarps - 1) / kWarps;
     const int grid = static_cast<int>(std::max<std::size_t>(
         1, std::min<std::size_t>(teams, static_cast<std::size_t>(setup.sms) *
                                             std::max(setup.occupancy[index], 1))));
-    Check(LaunchLinearTyped<float, float>(kmax, kLinearForward, args, grid, stream, nullptr),
+    Check(LaunchLinearF32(false, kmax, kLinearForward, args, grid, stream, nullptr),
           "tree-HMM accelerator kernel launch");
     return THMM_OK;
   } catch (const std::invalid_argument &error) {
