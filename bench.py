@@ -466,6 +466,9 @@ def run_ours(args, rank, world, local_rank, dist):
                 "call_ms_median": statistics.median(call_ms),
                 "call_ms": [round(v, 3) for v in call_ms],
                 "api_wall_ms": [round(v, 3) for v in api_wall_ms],
+                "api_upload_ms": [round(v, 3) for v in api_upload_ms],
+                "api_kernel_ms": [round(v, 3) for v in api_kernel_ms],
+                "api_download_ms": [round(v, 3) for v in api_download_ms],
                 "stripes": ws.launches // 2},
         "gpu_launches": args.steps * launches_per_step,
         "clocks": sampler.summary(),

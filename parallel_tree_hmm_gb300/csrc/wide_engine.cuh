@@ -17,9 +17,8 @@
 // divided by an exact power of two, exponents are summed in an integer and
 // log Z = ln2 * sum + log(sum(root)) is formed in FP64.
 //
-// Shared memory: four 32 KB operand buffers (X hi/lo, Y hi/lo for a product
-// depth of 64) plus a few K-vectors, so one CTA runs per SM and it may hold
-// all 512 tensor-memory columns. Every tensor-core wait is bounded; a wait
+// Shared memory: four operand buffers (X hi/lo, Y hi/lo for a product depth
+// of 64) plus a few K-vectors; one CTA per SM (see Layout). Every tensor-core wait is bounded; a wait
 // that gives up sets kErrorTensorTimeout and the host reports an error.
 #ifndef THMM_WIDE_ENGINE_CUH_
 #define THMM_WIDE_ENGINE_CUH_
@@ -35,14 +34,31 @@ namespace thmm {
 namespace wide {
 
 constexpr unsigned kThreads = 128;
-constexpr unsigned kChunk = 64;                      // product depth staged at once
-constexpr unsigned kOperandBytes = 128 * kChunk * 4; // one hi or lo operand (32 KB)
-constexpr std::uint32_t kSbo = kChunk / 4 * 128;     // 2048 bytes between 8-row groups
-constexpr unsigned kVectors = 6;                     // K-vectors of 128 floats
-constexpr unsigned kSmemBytes = 4 * kOperandBytes + kVectors * 128 * 4;
-constexpr std::uint32_t kTmemColumns = 512;
-// Tensor-memory columns of the three accumulators of a reverse compression.
-constexpr std::uint32_t kProductColumn = 0, kLeftColumn = 128, kRightColumn = 256;
+constexpr unsigned kChunk = 64;                  // product depth staged at once
+constexpr std::uint32_t kSbo = kChunk / 4 * 128; // 2048 bytes between 8-row groups
+constexpr unsigned kVectors = 6;                 // K-vectors of 128 floats
+
+// Shared- and tensor-memory layout for padded state count KP. X operands
+// have M = 128 rows, Y operands N = KP rows, both a depth chunk of 64; the
+// three accumulators of a reverse compression sit at columns 0, KP and 2 KP.
+// One CTA per SM holds all 512 TMEM columns: the dynamic shared memory is
+// padded to more than half of the SM's 228 KB so that a second CTA cannot
+// be resident (and wait on the allocation). Two CTAs per SM at KP = 64 (99 KB
+// each, 256 columns) measured slower: the shared-memory carve-out left the
+// operand-staging loads too little L1.
+template <int KP> struct Layout {
+  static constexpr unsigned kXBytes = 128 * kChunk * 4;
+  static constexpr unsigned kYBytes = KP * kChunk * 4;
+  static constexpr unsigned kXh = 0, kXl = kXBytes;
+  static constexpr unsigned kYh = 2 * kXBytes, kYl = 2 * kXBytes + kYBytes;
+  static constexpr unsigned kVectorsAt = 2 * kXBytes + 2 * kYBytes;
+  static constexpr unsigned kUsedBytes = kVectorsAt + kVectors * 128 * 4;
+  static constexpr unsigned kSmemBytes = kUsedBytes > 116 * 1024 ? kUsedBytes : 116 * 1024;
+  static constexpr std::uint32_t kTmemColumns = 512;
+  static constexpr std::uint32_t kProductColumn = 0, kLeftColumn = KP, kRightColumn = 2 * KP;
+  static constexpr int kCtasPerSm = 1;
+  static_assert(2 * kSmemBytes > 228 * 1024, "a second CTA would wait on TMEM");
+};
 
 struct Shared {
   std::uint64_t barrier;
@@ -174,9 +190,9 @@ __device__ __forceinline__ void Stage(const Source &src, unsigned K, unsigned d0
 }
 
 // Clears the four operand buffers (once per launch).
-__device__ __forceinline__ void ClearOperands(unsigned char *smem) {
+template <int KP> __device__ __forceinline__ void ClearOperands(unsigned char *smem) {
   float4 *p = reinterpret_cast<float4 *>(smem);
-  for (unsigned i = threadIdx.x; i < 4 * kOperandBytes / 16; i += kThreads)
+  for (unsigned i = threadIdx.x; i < Layout<KP>::kVectorsAt / 16; i += kThreads)
     p[i] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
 }
 
@@ -188,10 +204,10 @@ template <int KP, class XS, class YS>
 __device__ bool Product(unsigned char *smem, Shared &sh, std::uint32_t &phase,
                         std::uint32_t tmem, unsigned K, const XS &x, const YS &y) {
   static_assert(KP % kChunk == 0 && KP <= 128, "padded state count");
-  unsigned char *const xh = smem;
-  unsigned char *const xl = smem + kOperandBytes;
-  unsigned char *const yh = smem + 2 * kOperandBytes;
-  unsigned char *const yl = smem + 3 * kOperandBytes;
+  unsigned char *const xh = smem + Layout<KP>::kXh;
+  unsigned char *const xl = smem + Layout<KP>::kXl;
+  unsigned char *const yh = smem + Layout<KP>::kYh;
+  unsigned char *const yl = smem + Layout<KP>::kYl;
   constexpr std::uint32_t kDescriptor = umma::Tf32Descriptor(128, KP);
   bool ok = true;
 #pragma unroll 1

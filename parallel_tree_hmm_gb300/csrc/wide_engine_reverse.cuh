@@ -87,7 +87,7 @@ template <int KP> __device__ void Tree<KP>::Reverse() {
         __syncthreads();
         const float *mid = middle;
         // Unnormalised output, recomputed: left * diag(middle) * right.
-        ok = Product<KP>(smem, sh, phase, tmem + kProductColumn, K,
+        ok = Product<KP>(smem, sh, phase, tmem + Layout<KP>::kProductColumn, K,
                          RowMajor{left, middle}, Transposed{right}) &&
              ok;
         // ratio = adjoint / output, written over the output adjoint (each
@@ -99,7 +99,7 @@ template <int KP> __device__ void Tree<KP>::Reverse() {
 #pragma unroll 1
         for (unsigned c = 0; c < KP; c += 32) {
           float row[32];
-          umma::Load32(tmem + kProductColumn + lane_base + c, row);
+          umma::Load32(tmem + Layout<KP>::kProductColumn + lane_base + c, row);
           if (j < K) {
 #pragma unroll
             for (unsigned q = 0; q < 32; ++q)
@@ -113,11 +113,11 @@ template <int KP> __device__ void Tree<KP>::Reverse() {
         __syncthreads();
         const float *ratio_matrix = output_adjoint;
         // P1[r][m] = sum_c ratio[r][c] right[m][c]  (left adjoint factor).
-        ok = Product<KP>(smem, sh, phase, tmem + kLeftColumn, K,
+        ok = Product<KP>(smem, sh, phase, tmem + Layout<KP>::kLeftColumn, K,
                          RowMajor{ratio_matrix, nullptr}, RowMajor{right, nullptr}) &&
              ok;
         // P2[m][c] = sum_r left[r][m] ratio[r][c]  (right adjoint factor).
-        ok = Product<KP>(smem, sh, phase, tmem + kRightColumn, K, Transposed{left},
+        ok = Product<KP>(smem, sh, phase, tmem + Layout<KP>::kRightColumn, K, Transposed{left},
                          Transposed{ratio_matrix}) &&
              ok;
         // Row j: left adjoint left[j][m] middle[m] P1[j][m]; right adjoint
@@ -128,8 +128,8 @@ template <int KP> __device__ void Tree<KP>::Reverse() {
 #pragma unroll 1
         for (unsigned c = 0; c < KP; c += 32) {
           float p1[32], p2[32];
-          umma::Load32(tmem + kLeftColumn + lane_base + c, p1);
-          umma::Load32(tmem + kRightColumn + lane_base + c, p2);
+          umma::Load32(tmem + Layout<KP>::kLeftColumn + lane_base + c, p1);
+          umma::Load32(tmem + Layout<KP>::kRightColumn + lane_base + c, p2);
           if (j < K) {
 #pragma unroll
             for (unsigned q = 0; q < 32; ++q) {
@@ -155,16 +155,17 @@ template <int KP> __device__ void Tree<KP>::Reverse() {
   __syncthreads();
 }
 
-// Persistent kernel: one CTA per SM, trees from the large-instance queue.
+// Persistent kernel: one or two CTAs per SM (Layout), trees from the
+// large-instance queue.
 template <int KP, int kPart>
-__global__ void __launch_bounds__(kThreads, 1) WideKernel(EngineArgs args) {
+__global__ void __launch_bounds__(kThreads, Layout<KP>::kCtasPerSm) WideKernel(EngineArgs args) {
   extern __shared__ __align__(1024) unsigned char dynamic_smem[];
   __shared__ Shared sh;
-  ClearOperands(dynamic_smem);
+  ClearOperands<KP>(dynamic_smem);
   if (threadIdx.x == 0)
     umma::BarrierInit(&sh.barrier);
   if (threadIdx.x < 32)
-    umma::Allocate(&sh.tmem, kTmemColumns);
+    umma::Allocate(&sh.tmem, Layout<KP>::kTmemColumns);
   umma::FenceBeforeSync();
   __syncthreads();
   umma::FenceAfterSync();
@@ -192,7 +193,7 @@ __global__ void __launch_bounds__(kThreads, 1) WideKernel(EngineArgs args) {
   __syncthreads();
   umma::FenceAfterSync();
   if (threadIdx.x < 32)
-    umma::Deallocate(tmem, kTmemColumns);
+    umma::Deallocate(tmem, Layout<KP>::kTmemColumns);
 }
 
 template <int KP, int kPart>
@@ -200,13 +201,13 @@ cudaError_t LaunchWidePart(const EngineArgs &args, int grid, cudaStream_t stream
                            int *blocks_per_sm) {
   auto kernel = WideKernel<KP, kPart>;
   const cudaError_t status = cudaFuncSetAttribute(
-      kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(kSmemBytes));
+      kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(Layout<KP>::kSmemBytes));
   if (status != cudaSuccess)
     return status;
   if (blocks_per_sm != nullptr)
     return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, kernel, kThreads,
-                                                         kSmemBytes);
-  kernel<<<grid, kThreads, kSmemBytes, stream>>>(args);
+                                                         Layout<KP>::kSmemBytes);
+  kernel<<<grid, kThreads, Layout<KP>::kSmemBytes, stream>>>(args);
   return cudaGetLastError();
 }
 

@@ -50,12 +50,12 @@ template <int KP> __device__ void Tree<KP>::Forward() {
         NodeVector(op.y, op.w, middle);
         __syncthreads();
         // X(r, d) = left[r][d] * middle[d]; Y(n, d) = right[d][n].
-        ok = Product<KP>(smem, sh, phase, tmem + kProductColumn, K,
+        ok = Product<KP>(smem, sh, phase, tmem + Layout<KP>::kProductColumn, K,
                          RowMajor{Path(op.x), middle}, Transposed{Path(op.z)}) &&
              ok;
         // Row j of the product is tensor-memory lane j: maximum, then scale.
         const std::uint32_t lane_base =
-            tmem + kProductColumn + ((threadIdx.x & ~31u) << 16);
+            tmem + Layout<KP>::kProductColumn + ((threadIdx.x & ~31u) << 16);
         float m = 0.0f;
 #pragma unroll 1
         for (unsigned c = 0; c < KP; c += 32) {

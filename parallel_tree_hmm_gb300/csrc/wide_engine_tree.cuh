@@ -42,7 +42,7 @@ template <int KP> struct Tree {
     comp_mu = comps + static_cast<std::size_t>(prog.num_compressions) * KK;
     edge_in = static_cast<const float *>(a.edge_in) +
               inst.edge_in_base * static_cast<std::uint64_t>(KK);
-    float *vectors = reinterpret_cast<float *>(smem + 4 * kOperandBytes);
+    float *vectors = reinterpret_cast<float *>(smem + Layout<KP>::kVectorsAt);
     v = vectors;
     leaf = vectors + 128;
     msg = vectors + 256;
