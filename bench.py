@@ -328,7 +328,9 @@ def run_ours(args, rank, world, local_rank, dist):
     torch.cuda.set_device(device)
     forest = Forest(args.trees, args.states, rank_seed(args.seed, rank))
     K = forest.states
-    plans = [thmm.Plan(p) for p in forest.parents]
+    setup_start = time.perf_counter()
+    plans = thmm.Plan.many(forest.parents)
+    plan_s = time.perf_counter() - setup_start
     factor_sets = [forest.factors(rank_seed(args.seed, rank) + 1 + i) for i in range(2)]
     observations = forest.observations()
 
@@ -346,7 +348,9 @@ def run_ours(args, rank, world, local_rank, dist):
         staged.edge_potentials[:] = edges
         return staged
 
+    reserve_start = time.perf_counter()
     ws = reserve(np.float32)
+    reserve_s = time.perf_counter() - reserve_start
     staged = stage(ws, factor_sets[0])
     staged.observations[:] = observations
     first = ws.posterior_marginals_prepared(staged, thmm.CategoricalInputUpdate.kAll)
@@ -451,6 +455,7 @@ def run_ours(args, rank, world, local_rank, dist):
                    "chosen_over_plain_fp64": value / plain_value,
                    "plain_fp64_log_z_rel_diff": plain_logz_diff,
                    "tuning": tuning, "plain_fp64_tuning": plain_tuning,
+                   "host_plan_s": plan_s, "reserve_s": reserve_s,
                    "node_marginal_normalisation_error": normalisation_error},
         "roofline": {"bound": "hbm", "achieved": achieved,
                      "peak": peak, "unit": "GB/s", "frac": achieved / peak,
@@ -583,7 +588,7 @@ def run_gw(args, rank, world, local_rank, dist):
 
     device = local_rank
     torch.cuda.set_device(device)
-    plans = [thmm.Plan(p) for p in forest.parents]
+    plans = thmm.Plan.many(forest.parents)
     ws = thmm.Workspace()
     ws.reserve_forest_categorical(plans, K, K, forest.observed, device,
                                   kind="maximum,sampling", scalar=np.float32)
@@ -700,7 +705,7 @@ def run_dense(args, rank, world, local_rank, dist):
     K = args.states
     rng = np.random.default_rng(rank_seed(args.seed, rank))
     parents = [synthetic.spine_heavy(rng, args.tree_nodes) for _ in range(args.trees)]
-    plans = [thmm.Plan(p) for p in parents]
+    plans = thmm.Plan.many(parents)
     total_nodes = sum(p.num_nodes for p in plans)
     total_edges = sum(p.num_edges for p in plans)
     compressions = sum(int(p.num_compressions) for p in plans)

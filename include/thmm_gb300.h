@@ -110,6 +110,13 @@ typedef struct {
 /* btrc::MakePlan(parents) (consumed at tests/accelerator_test.h:19-20). */
 thmm_status thmm_plan_create(const int64_t *parents, size_t count,
                              thmm_plan **out);
+/* Extension (no reference counterpart): the plans of `tree_count` trees at
+ * once, built on `threads` host threads (0: all hardware threads). Tree t's
+ * parent array is parents[offsets[t] .. offsets[t + 1]). On error no plan is
+ * returned (every out[t] is null) and the status is that of the lowest
+ * failing tree, as thmm_plan_create would report it. */
+thmm_status thmm_plan_create_many(const int64_t *parents, const size_t *offsets,
+                                  size_t tree_count, unsigned threads, thmm_plan **out);
 void thmm_plan_destroy(thmm_plan *plan);
 thmm_status thmm_plan_get_info(const thmm_plan *plan, thmm_plan_info *out);
 thmm_status thmm_plan_get_arrays(const thmm_plan *plan, thmm_plan_arrays *out);

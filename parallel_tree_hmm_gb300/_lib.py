@@ -120,6 +120,8 @@ PROTOTYPES = {
     "thmm_last_error": (ctypes.c_char_p, []),
     "thmm_plan_create": (c_int, [ctypes.POINTER(ctypes.c_int64), c_size,
                                  ctypes.POINTER(c_void_p)]),
+    "thmm_plan_create_many": (c_int, [ctypes.POINTER(ctypes.c_int64), ctypes.POINTER(c_size),
+                                      c_size, ctypes.c_uint, ctypes.POINTER(c_void_p)]),
     "thmm_plan_destroy": (None, [c_void_p]),
     "thmm_plan_get_info": (c_int, [c_void_p, ctypes.POINTER(PlanInfo)]),
     "thmm_plan_get_arrays": (c_int, [c_void_p, ctypes.POINTER(PlanArrays)]),

@@ -78,14 +78,16 @@ class CategoricalInputUpdate(enum.IntEnum):
 class Plan:
     """btrc::MakePlan(parents): the rake/compress plan of one tree."""
 
-    def __init__(self, parents: Sequence[int]):
+    def __init__(self, parents: Sequence[int] | None = None, *, _handle: int | None = None):
         lib = library()
-        parents = np.ascontiguousarray(parents, dtype=np.int64)
-        handle = ctypes.c_void_p()
-        _check(lib.thmm_plan_create(
-            parents.ctypes.data_as(ctypes.POINTER(ctypes.c_int64)), parents.size,
-            ctypes.byref(handle)))
-        self._handle = handle.value
+        if _handle is None:
+            parents = np.ascontiguousarray(parents, dtype=np.int64)
+            handle = ctypes.c_void_p()
+            _check(lib.thmm_plan_create(
+                parents.ctypes.data_as(ctypes.POINTER(ctypes.c_int64)), parents.size,
+                ctypes.byref(handle)))
+            _handle = handle.value
+        self._handle = _handle
         self._lib = lib
         info = _lib.PlanInfo()
         _check(lib.thmm_plan_get_info(self._handle, ctypes.byref(info)))
@@ -99,6 +101,22 @@ class Plan:
         self.num_rounds = info.num_rounds
         self.root = info.root
         self._arrays = None
+
+    @classmethod
+    def many(cls, parent_arrays: Sequence[Sequence[int]], threads: int = 0) -> list["Plan"]:
+        """Plans of many trees built on `threads` host threads (0: all)."""
+        lib = library()
+        arrays = [np.ascontiguousarray(p, dtype=np.int64) for p in parent_arrays]
+        offsets = np.zeros(len(arrays) + 1, dtype=np.uintp)
+        offsets[1:] = np.cumsum([a.size for a in arrays])
+        flat = (np.concatenate(arrays) if arrays else np.zeros(0, dtype=np.int64))
+        flat = np.ascontiguousarray(flat, dtype=np.int64)
+        handles = (ctypes.c_void_p * max(1, len(arrays)))()
+        _check(lib.thmm_plan_create_many(
+            flat.ctypes.data_as(ctypes.POINTER(ctypes.c_int64)),
+            offsets.ctypes.data_as(ctypes.POINTER(ctypes.c_size_t)), len(arrays), threads,
+            handles))
+        return [cls(_handle=handles[t]) for t in range(len(arrays))]
 
     _WIDTHS = {"edge_parents": ("num_edges", 1), "edge_children": ("num_edges", 1),
                "rakes": ("num_branches", 4), "combinations": ("num_combinations", 3),

@@ -18,11 +18,13 @@
 #include <cstdlib>
 #include <cstdio>
 #include <cstring>
+#include <exception>
 #include <limits>
 #include <memory>
 #include <numeric>
 #include <stdexcept>
 #include <string>
+#include <thread>
 #include <tuple>
 #include <unordered_map>
 #include <utility>
@@ -1252,6 +1254,56 @@ thmm_status thmm_plan_create(const int64_t *parents, size_t count,
     auto plan = std::make_unique<btrc::Plan>(
         btrc::MakePlan(std::span<const std::int64_t>(parents, count)));
     *out = reinterpret_cast<thmm_plan *>(plan.release());
+  });
+}
+
+thmm_status thmm_plan_create_many(const int64_t *parents, const size_t *offsets,
+                                  size_t tree_count, unsigned threads, thmm_plan **out) {
+  return Guard([&] {
+    if (out == nullptr || offsets == nullptr || (tree_count != 0 && parents == nullptr))
+      throw std::invalid_argument("plan arguments must not be null");
+    for (size_t t = 0; t < tree_count; ++t) {
+      out[t] = nullptr;
+      if (offsets[t + 1] < offsets[t])
+        throw std::invalid_argument("plan offsets must not decrease");
+    }
+    unsigned workers = threads != 0 ? threads : std::thread::hardware_concurrency();
+    workers = static_cast<unsigned>(
+        std::max<size_t>(1, std::min<size_t>(workers == 0 ? 1 : workers, tree_count)));
+    // Trees are dealt round-robin; each worker keeps the first error it meets.
+    std::vector<std::exception_ptr> errors(workers);
+    std::vector<size_t> failed(workers, tree_count);
+    const auto work = [&](unsigned w) {
+      for (size_t t = w; t < tree_count; t += workers) {
+        try {
+          auto plan = std::make_unique<btrc::Plan>(btrc::MakePlan(std::span<const std::int64_t>(
+              parents + offsets[t], offsets[t + 1] - offsets[t])));
+          out[t] = reinterpret_cast<thmm_plan *>(plan.release());
+        } catch (...) {
+          errors[w] = std::current_exception();
+          failed[w] = t;
+          return;
+        }
+      }
+    };
+    std::vector<std::thread> pool;
+    for (unsigned w = 1; w < workers; ++w)
+      pool.emplace_back(work, w);
+    work(0);
+    for (std::thread &thread : pool)
+      thread.join();
+    // Report the error of the lowest failing tree and release everything.
+    unsigned first = workers;
+    for (unsigned w = 0; w < workers; ++w)
+      if (errors[w] && (first == workers || failed[w] < failed[first]))
+        first = w;
+    if (first != workers) {
+      for (size_t t = 0; t < tree_count; ++t) {
+        delete reinterpret_cast<btrc::Plan *>(out[t]);
+        out[t] = nullptr;
+      }
+      std::rethrow_exception(errors[first]);
+    }
   });
 }
 

@@ -87,3 +87,25 @@ def test_compression_happens_on_the_five_node_tree(thmm):
 def test_invalid_trees_are_rejected(parents, thmm):
     with pytest.raises(thmm.InvalidArgument):
         thmm.Plan(np.array(parents, dtype=np.int64))
+
+
+def test_plans_built_in_parallel_match_single_builds(thmm):
+    rng = np.random.default_rng(31)
+    parents = [synthetic.random_recursive(rng, int(n)) for n in (1, 2, 50, 700, 3000)]
+    parents += [synthetic.caterpillar(400), synthetic.spine_heavy(rng, 900)]
+    for threads in (0, 1, 3):
+        many = thmm.Plan.many(parents, threads=threads)
+        assert len(many) == len(parents)
+        for p, plan in zip(parents, many):
+            single = thmm.Plan(p)
+            assert plan.num_nodes == single.num_nodes
+            assert plan.root == single.root
+            for name in ("rakes", "compressions", "batches", "edge_children"):
+                assert np.array_equal(getattr(plan, name), getattr(single, name))
+    assert thmm.Plan.many([]) == []
+
+
+def test_parallel_plan_errors_name_the_first_bad_tree(thmm):
+    good = np.array([-1, 0, 0])
+    with pytest.raises(thmm.InvalidArgument):
+        thmm.Plan.many([good, np.array([-1, 5]), good, np.array([0, 0])], threads=2)
