@@ -119,6 +119,29 @@ __device__ __forceinline__ bool Wait(std::uint64_t *barrier, std::uint32_t parit
   }
 }
 
+// Bulk (TMA, non-tensor) copies global -> shared completing on an mbarrier.
+// The issuing thread announces the bytes of the phase with ExpectBytes, then
+// issues the copies; every waiter uses Wait with the phase parity. Addresses
+// and sizes are multiples of 16 bytes.
+__device__ __forceinline__ void ExpectBytes(std::uint64_t *barrier, std::uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(
+                   SmemAddress(barrier)),
+               "r"(bytes)
+               : "memory");
+}
+__device__ __forceinline__ void BulkLoad(void *dst, const void *src, std::uint32_t bytes,
+                                         std::uint64_t *barrier) {
+  asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes "
+               "[%0], [%1], %2, [%3];" ::"r"(SmemAddress(dst)),
+               "l"(src), "r"(bytes), "r"(SmemAddress(barrier))
+               : "memory");
+}
+// Orders this thread's earlier generic-proxy memory accesses before later
+// async-proxy (TMA, tensor core) accesses of the same memory, and back.
+__device__ __forceinline__ void FenceProxy() {
+  asm volatile("fence.proxy.async;" ::: "memory");
+}
+
 // Loads 32 consecutive FP32 accumulator columns of this thread's TMEM lane
 // (warp w reads lanes 32w .. 32w + 31).
 __device__ __forceinline__ void Load32(std::uint32_t address, float (&out)[32]) {

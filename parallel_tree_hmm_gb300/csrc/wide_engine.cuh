@@ -52,7 +52,12 @@ template <int KP> struct Layout {
   static constexpr unsigned kXh = 0, kXl = kXBytes;
   static constexpr unsigned kYh = 2 * kXBytes, kYl = 2 * kXBytes + kYBytes;
   static constexpr unsigned kVectorsAt = 2 * kXBytes + 2 * kYBytes;
-  static constexpr unsigned kUsedBytes = kVectorsAt + kVectors * 128 * 4;
+  // At KP = 64, three raw K x K matrices (path versions and the adjoint)
+  // land in shared memory by bulk copy before they are split into operands.
+  static constexpr unsigned kRawCount = KP == 64 ? 3 : 0;
+  static constexpr unsigned kRawBytes = KP * KP * 4;
+  static constexpr unsigned kRawAt = kVectorsAt + kVectors * 128 * 4;
+  static constexpr unsigned kUsedBytes = kRawAt + kRawCount * kRawBytes;
   static constexpr unsigned kSmemBytes = kUsedBytes > 116 * 1024 ? kUsedBytes : 116 * 1024;
   static constexpr std::uint32_t kTmemColumns = 512;
   static constexpr std::uint32_t kProductColumn = 0, kLeftColumn = KP, kRightColumn = 2 * KP;
@@ -61,7 +66,8 @@ template <int KP> struct Layout {
 };
 
 struct Shared {
-  std::uint64_t barrier;
+  std::uint64_t barrier;      // tensor-core completion
+  std::uint64_t copy_barrier; // bulk-copy completion
   double root_sum;
   std::uint32_t tmem;
   unsigned item;

@@ -27,6 +27,10 @@ template <int KP> __device__ void Tree<KP>::Reverse() {
       for (unsigned i = 0; i < step.count; ++i) {
         const uint4 op = rakes[step.offset + i];
         const float *path = Path(op.x);
+        if (bulk) {
+          Fetch(path, nullptr, nullptr, 1);
+          path = raw[0];
+        }
         NodeVector(op.y, op.w, leaf);
         if (j < K)
           v[j] = node_out[static_cast<std::size_t>(op.z) * K + j]; // parent marginal
@@ -73,6 +77,7 @@ template <int KP> __device__ void Tree<KP>::Reverse() {
         // Leaf adjoint: leaf[c] * sum_r ratio[r] * path[r][c].
         if (j < K)
           node_out[static_cast<std::size_t>(op.y & kMask) * K + j] = leaf[j] * msg[j];
+        umma::FenceProxy(); // path adjoints may later arrive by bulk copy
         __syncthreads();
       }
     } else if (step.kind == kStepCompress) {
@@ -83,6 +88,16 @@ template <int KP> __device__ void Tree<KP>::Reverse() {
         const float *left = Path(op.x);
         const float *right = Path(op.z);
         float *output_adjoint = comp_mu + static_cast<std::size_t>(tape) * KK;
+        float *left_out_base = adjoint_of(op.x);
+        float *right_out_base = adjoint_of(op.z);
+        if (bulk) {
+          // Left and right path versions and this compression's output
+          // adjoint; the ratio below then lives in shared memory only.
+          Fetch(left, right, output_adjoint, 3);
+          left = raw[0];
+          right = raw[1];
+          output_adjoint = raw[2];
+        }
         NodeVector(op.y, op.w, middle);
         __syncthreads();
         const float *mid = middle;
@@ -122,8 +137,8 @@ template <int KP> __device__ void Tree<KP>::Reverse() {
              ok;
         // Row j: left adjoint left[j][m] middle[m] P1[j][m]; right adjoint
         // right[j][c] middle[j] P2[j][c]; middle adjoint sum_c of the latter.
-        float *left_out = adjoint_of(op.x) + static_cast<std::size_t>(j) * K;
-        float *right_out = adjoint_of(op.z) + static_cast<std::size_t>(j) * K;
+        float *left_out = left_out_base + static_cast<std::size_t>(j) * K;
+        float *right_out = right_out_base + static_cast<std::size_t>(j) * K;
         float total = 0.0f;
 #pragma unroll 1
         for (unsigned c = 0; c < KP; c += 32) {
@@ -145,6 +160,7 @@ template <int KP> __device__ void Tree<KP>::Reverse() {
         }
         if (j < K)
           node_out[static_cast<std::size_t>(op.y & kMask) * K + j] = total;
+        umma::FenceProxy(); // path adjoints may later arrive by bulk copy
         umma::FenceBeforeSync();
         __syncthreads();
       }
@@ -162,15 +178,17 @@ __global__ void __launch_bounds__(kThreads, Layout<KP>::kCtasPerSm) WideKernel(E
   extern __shared__ __align__(1024) unsigned char dynamic_smem[];
   __shared__ Shared sh;
   ClearOperands<KP>(dynamic_smem);
-  if (threadIdx.x == 0)
+  if (threadIdx.x == 0) {
     umma::BarrierInit(&sh.barrier);
+    umma::BarrierInit(&sh.copy_barrier);
+  }
   if (threadIdx.x < 32)
     umma::Allocate(&sh.tmem, Layout<KP>::kTmemColumns);
   umma::FenceBeforeSync();
   __syncthreads();
   umma::FenceAfterSync();
   const std::uint32_t tmem = sh.tmem;
-  std::uint32_t phase = 0;
+  std::uint32_t phase = 0, copy_phase = 0;
   for (;;) {
     if (threadIdx.x == 0)
       sh.item = atomicAdd(&args.queue[0], 1u);
@@ -180,7 +198,7 @@ __global__ void __launch_bounds__(kThreads, Layout<KP>::kCtasPerSm) WideKernel(E
     if (index >= args.big_count)
       break;
     const unsigned item = args.big_items[index];
-    Tree<KP> tree(args, item, sh, dynamic_smem, tmem, phase);
+    Tree<KP> tree(args, item, sh, dynamic_smem, tmem, phase, copy_phase);
     if constexpr (kPart == kLinearForward) {
       tree.Forward();
       tree.Finish(item);

@@ -27,8 +27,13 @@ template <int KP> __device__ void Tree<KP>::Forward() {
         for (unsigned k = 0; k < op.w; ++k) {
           const uint4 rake = rakes[op.z + k];
           NodeVector(rake.y, rake.w, leaf);
+          const float *path = Path(rake.x);
+          if (bulk) {
+            Fetch(path, nullptr, nullptr, 1);
+            path = raw[0];
+          }
           __syncthreads();
-          MatVec(Path(rake.x), leaf, msg);
+          MatVec(path, leaf, msg);
           __syncthreads();
           const float message = j < K ? msg[j] : 0.0f;
           int e = Renormaliser(message);
@@ -48,10 +53,17 @@ template <int KP> __device__ void Tree<KP>::Forward() {
         const unsigned tape = g - prog.compress_base;
         const uint4 op = compress[g];
         NodeVector(op.y, op.w, middle);
+        const float *left = Path(op.x);
+        const float *right = Path(op.z);
+        if (bulk) {
+          Fetch(left, right, nullptr, 2);
+          left = raw[0];
+          right = raw[1];
+        }
         __syncthreads();
         // X(r, d) = left[r][d] * middle[d]; Y(n, d) = right[d][n].
         ok = Product<KP>(smem, sh, phase, tmem + Layout<KP>::kProductColumn, K,
-                         RowMajor{Path(op.x), middle}, Transposed{Path(op.z)}) &&
+                         RowMajor{left, middle}, Transposed{right}) &&
              ok;
         // Row j of the product is tensor-memory lane j: maximum, then scale.
         const std::uint32_t lane_base =
@@ -77,6 +89,8 @@ template <int KP> __device__ void Tree<KP>::Forward() {
             if (j < K && c + q < K)
               out[c + q] = ScalePow2(row[q], -e);
         }
+        // The compressed path may later arrive by bulk copy (async proxy).
+        umma::FenceProxy();
         umma::FenceBeforeSync();
         __syncthreads();
       }

@@ -14,6 +14,7 @@ template <int KP> struct Tree {
   unsigned char *smem;
   std::uint32_t tmem;
   std::uint32_t &phase;
+  std::uint32_t &copy_phase;
   DevInstance inst;
   DevProgram prog;
   unsigned K, KK;
@@ -25,12 +26,17 @@ template <int KP> struct Tree {
   float *v, *leaf, *msg, *middle, *ratio, *spare;
   long long exponent = 0; // thread 0's log-scale exponent sum
   int zero = 0;           // some renormalised message was identically zero
-  bool ok = true;         // every tensor-core wait completed
+  bool ok = true;         // every tensor-core and bulk-copy wait completed
+  // Raw K x K matrices in shared memory, filled by bulk copy (KP = 64 and K a
+  // multiple of 4, so every matrix is 16-byte aligned and sized).
+  float *raw[3] = {nullptr, nullptr, nullptr};
+  bool bulk = false;
 
   __device__ Tree(const EngineArgs &args, unsigned item, Shared &shared,
                   unsigned char *dynamic_smem, std::uint32_t tmem_base,
-                  std::uint32_t &mma_phase)
-      : a(args), sh(shared), smem(dynamic_smem), tmem(tmem_base), phase(mma_phase) {
+                  std::uint32_t &mma_phase, std::uint32_t &bulk_phase)
+      : a(args), sh(shared), smem(dynamic_smem), tmem(tmem_base), phase(mma_phase),
+        copy_phase(bulk_phase) {
     inst = a.instances[item];
     prog = a.programs[inst.program];
     K = a.states;
@@ -49,6 +55,31 @@ template <int KP> struct Tree {
     middle = vectors + 384;
     ratio = vectors + 512;
     spare = vectors + 640;
+    if constexpr (Layout<KP>::kRawCount == 3) {
+      for (int i = 0; i < 3; ++i)
+        raw[i] = reinterpret_cast<float *>(smem + Layout<KP>::kRawAt +
+                                           i * Layout<KP>::kRawBytes);
+      bulk = K % 4 == 0 && (reinterpret_cast<std::uintptr_t>(edge_in) & 15) == 0 &&
+             (reinterpret_cast<std::uintptr_t>(comps) & 15) == 0 &&
+             (reinterpret_cast<std::uintptr_t>(comp_mu) & 15) == 0;
+    }
+  }
+
+  // Copies `count` K x K matrices into raw[0 .. count) with one bulk copy each
+  // and waits (bounded) for all of them. Every thread calls it; the raw
+  // buffers must be free (all earlier reads behind a CTA barrier).
+  __device__ __forceinline__ void Fetch(const float *m0, const float *m1, const float *m2,
+                                        unsigned count) {
+    const std::uint32_t bytes = KK * 4u;
+    if (threadIdx.x == 0) {
+      umma::FenceProxy();
+      umma::ExpectBytes(&sh.copy_barrier, bytes * count);
+      const float *sources[3] = {m0, m1, m2};
+      for (unsigned i = 0; i < count; ++i)
+        umma::BulkLoad(raw[i], sources[i], bytes, &sh.copy_barrier);
+    }
+    ok = umma::Wait(&sh.copy_barrier, copy_phase) && ok;
+    copy_phase ^= 1u;
   }
 
   // Row r of path version `ref` (input edge, or compressed path kFlag | t).
