@@ -66,6 +66,12 @@ def parse_args():
                              "spine-heavy trees, K = 64 or 128, tensor-core marginals")
     parser.add_argument("--tree-nodes", type=int, default=None,
                         help="dense workload: nodes per tree")
+    parser.add_argument("--shape", choices=["spine-heavy", "recursive"], default="spine-heavy",
+                        help="dense workload: tree shape")
+    parser.add_argument("--edge-sigma", type=float, default=2.0,
+                        help="dense workload: edge factors lognormal(0, sigma)")
+    parser.add_argument("--zero-fraction", type=float, default=0.05,
+                        help="dense workload: fraction of exactly zero edge entries")
     args = parser.parse_args()
     if args.workload == "gw":
         if args.trees == 4096:
@@ -692,42 +698,46 @@ def run_gw(args, rank, world, local_rank, dist):
 
 # -------------------------------------------- dense-contraction workload
 def run_dense(args, rank, world, local_rank, dist):
-    """Spine-heavy random recursive trees (node i attaches to i - 1 with
-    probability 0.95, else to a uniform earlier node), K = 64 or 128, dense
-    node factors lognormal(0, 1), edge factors lognormal(0, 2) with 5% exact
-    zeros; log Z and all marginals on the tensor-core engine. The trees are
-    scaled down from 100,000 nodes so that the edge factors fit in HBM and
-    host memory (--tree-nodes)."""
+    """Dense-factor marginals. Default: spine-heavy random recursive trees
+    (node i attaches to i - 1 with probability 0.95, else to a uniform earlier
+    node), K = 64 or 128, node factors lognormal(0, 1), edge factors
+    lognormal(0, 2) with 5% exact zeros, on the tensor-core engine; the trees
+    are scaled down from 100,000 nodes so that the edge factors fit in HBM and
+    host memory (--tree-nodes). With --shape recursive --states 20
+    --tree-nodes 5000 --trees 1024 --edge-sigma 1.5 --zero-fraction 0.02 it is
+    the differentiation workload (gradient = marginals) at full size."""
     import parallel_tree_hmm_gb300 as thmm
     from oracle import bridge
     from parallel_tree_hmm_gb300 import synthetic
 
     K = args.states
     rng = np.random.default_rng(rank_seed(args.seed, rank))
-    parents = [synthetic.spine_heavy(rng, args.tree_nodes) for _ in range(args.trees)]
+    grow = synthetic.spine_heavy if args.shape == "spine-heavy" else synthetic.random_recursive
+    parents = [grow(rng, args.tree_nodes) for _ in range(args.trees)]
     plans = thmm.Plan.many(parents)
     total_nodes = sum(p.num_nodes for p in plans)
     total_edges = sum(p.num_edges for p in plans)
     compressions = sum(int(p.num_compressions) for p in plans)
     config = {
-        "workload": (f"dense contractions: {args.trees} spine-heavy trees of {args.tree_nodes} "
-                     f"nodes (spine probability 0.95), K={K}, lognormal(0,1) node and "
-                     f"lognormal(0,2) edge factors with 5% zeros, marginals"),
+        "workload": (f"dense factors: {args.trees} {args.shape} trees of {args.tree_nodes} "
+                     f"nodes, K={K}, lognormal(0,1) node and lognormal(0,{args.edge_sigma:g}) "
+                     f"edge factors with {100 * args.zero_fraction:g}% zeros, marginals"),
         "trees": args.trees, "nodes_per_rank": total_nodes, "states": K,
         "compressions_per_rank": compressions, "seed": args.seed,
         "parallelism": f"replicas per GPU x{args.gpus}",
         "l2": "inputs larger than L2 (edge factors of one step > 129 MB)",
-        "scaled_from": "256 trees x 100,000 nodes (1.7 TB of edge factors at K=128)",
+        "scaled_from": ("256 trees x 100,000 nodes (1.7 TB of edge factors at K=128)"
+                        if args.shape == "spine-heavy" else None),
     }
-    metric = "tree-nodes/s for logZ+marginals+grad (dense contractions)"
+    metric = "tree-nodes/s for logZ+marginals+grad (dense factors)"
 
     def edge_chunks(fill):
         chunk = 1 << 24
         values = total_edges * K * K
         for start in range(0, values, chunk):
             n = min(chunk, values - start)
-            block = np.exp(2.0 * rng.standard_normal(n, dtype=np.float32))
-            block[rng.random(n, dtype=np.float32) < 0.05] = 0.0
+            block = np.exp(np.float32(args.edge_sigma) * rng.standard_normal(n, dtype=np.float32))
+            block[rng.random(n, dtype=np.float32) < args.zero_fraction] = 0.0
             fill(start, block)
 
     node_factors = np.exp(rng.standard_normal(total_nodes * K, dtype=np.float32))
@@ -832,10 +842,12 @@ def run_dense(args, rank, world, local_rank, dist):
         "metric": metric, "value": value, "unit": UNIT, "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": step_ms,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-        "dtype": "f32 (3xTF32 tensor-core products)", "data": "synthetic",
+        "dtype": "f32 (3xTF32 tensor-core products)" if K > 32 else "f32",
+        "data": "synthetic",
         "config": {**config, "all_log_z_finite": finite,
                    "node_marginal_normalisation_error": node_sum_error,
-                   "useful_tensor_tflops": useful_flops / (step_ms / 1e3) / 1e12},
+                   ("useful_tensor_tflops" if K > 32 else "useful_product_tflops"):
+                       useful_flops / (step_ms / 1e3) / 1e12},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak,
                      "peak_source": "measured" if peaks else "fallback",

@@ -355,3 +355,41 @@ def test_galton_watson_categorical_map_and_sampling_bit_exact(gpu):
                              bridge.MATH_PORTABLE)
         assert np.array_equal(sample_states[node0:node0 + n], draw)
         node0 += n
+
+
+def test_plain_method_configuration(gpu):
+    """The reference's CPU-runnable case: 64 binary trees of 999 nodes grown by
+    uniform leaf splitting, K = 4, Dirichlet(1) root factor and edge rows,
+    byte observations on the leaves with a Dirichlet(5) emission table,
+    all-ones internal factors; log Z and marginals for every tree against the
+    FP64 oracle (FP32 arithmetic)."""
+    rng = np.random.default_rng(1999)
+    K, trees = 4, 64
+    parents = [synthetic.leaf_splitting(rng, 999) for _ in range(trees)]
+    plans = gpu.Plan.many(parents)
+    observed = [synthetic.leaves(p) for p in parents]
+    root = synthetic.dirichlet_rows(rng, 1, K, 1.0, np.float32).ravel()
+    emission = synthetic.dirichlet_rows(rng, K, K, 5.0, np.float32)
+    edges = [synthetic.dirichlet_rows(rng, (len(p) - 1) * K, K, 1.0, np.float32).ravel()
+             for p in parents]
+    obs = [rng.integers(0, K, len(o), dtype=np.uint8) for o in observed]
+    ws = gpu.Workspace()
+    ws.reserve_forest_categorical(plans, K, K, observed, kind="marginals", scalar=np.float32)
+    staged = ws.categorical_inputs()
+    staged.root_potential[:] = root
+    staged.emission_potentials[:] = emission.ravel()
+    staged.edge_potentials[:] = np.concatenate(edges)
+    staged.observations[:] = np.concatenate(obs)
+    view = ws.posterior_marginals_prepared(staged, gpu.CategoricalInputUpdate.kAll)
+    n0 = e0 = 0
+    for t, plan in enumerate(plans):
+        n, e = plan.num_nodes, plan.num_edges
+        dense = np.ones((n, K), dtype=np.float32)
+        dense[plan.root] = root
+        dense[observed[t]] = dense[observed[t]] * emission[obs[t]]
+        log_z, _, node_m, edge_m = bridge.marginals(
+            plan, K, dense.astype(np.float64).ravel(), edges[t].astype(np.float64))
+        assert abs(view.log_partitions[t] - log_z) <= 1e-6 * max(1, abs(log_z))
+        assert np.max(np.abs(view.nodes[n0 * K:(n0 + n) * K] - node_m)) <= 1e-5
+        assert np.max(np.abs(view.edges[e0 * K * K:(e0 + e) * K * K] - edge_m)) <= 1e-5
+        n0, e0 = n0 + n, e0 + e
