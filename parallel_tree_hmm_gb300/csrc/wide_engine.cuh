@@ -52,9 +52,10 @@ template <int KP> struct Layout {
   static constexpr unsigned kXh = 0, kXl = kXBytes;
   static constexpr unsigned kYh = 2 * kXBytes, kYl = 2 * kXBytes + kYBytes;
   static constexpr unsigned kVectorsAt = 2 * kXBytes + 2 * kYBytes;
-  // At KP = 64, three raw K x K matrices (path versions and the adjoint)
-  // land in shared memory by bulk copy before they are split into operands.
-  static constexpr unsigned kRawCount = KP == 64 ? 3 : 0;
+  // At KP = 64, two sets of three raw K x K matrices (path versions and the
+  // adjoint): one set feeds the current operation while the bulk copy of the
+  // next operation's set is in flight.
+  static constexpr unsigned kRawCount = KP == 64 ? 6 : 0;
   static constexpr unsigned kRawBytes = KP * KP * 4;
   static constexpr unsigned kRawAt = kVectorsAt + kVectors * 128 * 4;
   static constexpr unsigned kUsedBytes = kRawAt + kRawCount * kRawBytes;
@@ -66,8 +67,8 @@ template <int KP> struct Layout {
 };
 
 struct Shared {
-  std::uint64_t barrier;      // tensor-core completion
-  std::uint64_t copy_barrier; // bulk-copy completion
+  std::uint64_t barrier;         // tensor-core completion
+  std::uint64_t copy_barrier[2]; // bulk-copy completion, one per raw set
   double root_sum;
   std::uint32_t tmem;
   unsigned item;

@@ -28,7 +28,9 @@ template <int KP> __device__ void Tree<KP>::Reverse() {
         const uint4 op = rakes[step.offset + i];
         const float *path = Path(op.x);
         if (bulk) {
-          Fetch(path, nullptr, nullptr, 1);
+          const bool has_next = i + 1 < step.count;
+          const float *next = has_next ? Path(rakes[step.offset + i + 1].x) : nullptr;
+          Fetch(path, nullptr, nullptr, 1, has_next, next, nullptr, nullptr);
           path = raw[0];
         }
         NodeVector(op.y, op.w, leaf);
@@ -93,7 +95,10 @@ template <int KP> __device__ void Tree<KP>::Reverse() {
         if (bulk) {
           // Left and right path versions and this compression's output
           // adjoint; the ratio below then lives in shared memory only.
-          Fetch(left, right, output_adjoint, 3);
+          const bool has_next = i + 1 < step.count;
+          const uint4 next = has_next ? compress[g + 1] : op;
+          Fetch(left, right, output_adjoint, 3, has_next, Path(next.x), Path(next.z),
+                comp_mu + static_cast<std::size_t>(tape + 1) * KK);
           left = raw[0];
           right = raw[1];
           output_adjoint = raw[2];
@@ -180,7 +185,8 @@ __global__ void __launch_bounds__(kThreads, Layout<KP>::kCtasPerSm) WideKernel(E
   ClearOperands<KP>(dynamic_smem);
   if (threadIdx.x == 0) {
     umma::BarrierInit(&sh.barrier);
-    umma::BarrierInit(&sh.copy_barrier);
+    umma::BarrierInit(&sh.copy_barrier[0]);
+    umma::BarrierInit(&sh.copy_barrier[1]);
   }
   if (threadIdx.x < 32)
     umma::Allocate(&sh.tmem, Layout<KP>::kTmemColumns);

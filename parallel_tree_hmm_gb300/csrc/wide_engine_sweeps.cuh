@@ -29,7 +29,17 @@ template <int KP> __device__ void Tree<KP>::Forward() {
           NodeVector(rake.y, rake.w, leaf);
           const float *path = Path(rake.x);
           if (bulk) {
-            Fetch(path, nullptr, nullptr, 1);
+            // Next rake of this step: the following one of this gather, or
+            // the first one of the next gather.
+            const float *next = nullptr;
+            if (k + 1 < op.w) {
+              next = Path(rakes[op.z + k + 1].x);
+            } else if (i + 1 < step.count) {
+              const uint4 following = gathers[step.offset + i + 1];
+              if (following.w != 0)
+                next = Path(rakes[following.z].x);
+            }
+            Fetch(path, nullptr, nullptr, 1, next != nullptr, next, nullptr, nullptr);
             path = raw[0];
           }
           __syncthreads();
@@ -56,7 +66,9 @@ template <int KP> __device__ void Tree<KP>::Forward() {
         const float *left = Path(op.x);
         const float *right = Path(op.z);
         if (bulk) {
-          Fetch(left, right, nullptr, 2);
+          const bool has_next = i + 1 < step.count;
+          const uint4 next = has_next ? compress[g + 1] : op;
+          Fetch(left, right, nullptr, 2, has_next, Path(next.x), Path(next.z), nullptr);
           left = raw[0];
           right = raw[1];
         }

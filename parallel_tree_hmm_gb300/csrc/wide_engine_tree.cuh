@@ -14,7 +14,7 @@ template <int KP> struct Tree {
   unsigned char *smem;
   std::uint32_t tmem;
   std::uint32_t &phase;
-  std::uint32_t &copy_phase;
+  std::uint32_t &copy_phase; // bit s: phase parity of raw set s
   DevInstance inst;
   DevProgram prog;
   unsigned K, KK;
@@ -29,7 +29,10 @@ template <int KP> struct Tree {
   bool ok = true;         // every tensor-core and bulk-copy wait completed
   // Raw K x K matrices in shared memory, filled by bulk copy (KP = 64 and K a
   // multiple of 4, so every matrix is 16-byte aligned and sized).
-  float *raw[3] = {nullptr, nullptr, nullptr};
+  float *raw[3] = {nullptr, nullptr, nullptr}; // the current set
+  float *raw_base = nullptr;  // set s, matrix i at raw_base + (3 s + i) K_P^2
+  unsigned current = 0;       // raw set of the current operation
+  unsigned issued = 0;        // bit s: a copy into set s is in flight
   bool bulk = false;
 
   __device__ Tree(const EngineArgs &args, unsigned item, Shared &shared,
@@ -55,31 +58,60 @@ template <int KP> struct Tree {
     middle = vectors + 384;
     ratio = vectors + 512;
     spare = vectors + 640;
-    if constexpr (Layout<KP>::kRawCount == 3) {
-      for (int i = 0; i < 3; ++i)
-        raw[i] = reinterpret_cast<float *>(smem + Layout<KP>::kRawAt +
-                                           i * Layout<KP>::kRawBytes);
+    if constexpr (Layout<KP>::kRawCount == 6) {
+      raw_base = reinterpret_cast<float *>(smem + Layout<KP>::kRawAt);
       bulk = K % 4 == 0 && (reinterpret_cast<std::uintptr_t>(edge_in) & 15) == 0 &&
              (reinterpret_cast<std::uintptr_t>(comps) & 15) == 0 &&
              (reinterpret_cast<std::uintptr_t>(comp_mu) & 15) == 0;
     }
   }
 
-  // Copies `count` K x K matrices into raw[0 .. count) with one bulk copy each
-  // and waits (bounded) for all of them. Every thread calls it; the raw
-  // buffers must be free (all earlier reads behind a CTA barrier).
-  __device__ __forceinline__ void Fetch(const float *m0, const float *m1, const float *m2,
-                                        unsigned count) {
+  // Starts bulk copies of `count` K x K matrices into raw set `set` (thread 0
+  // only; the set must be free: its earlier readers are behind a CTA barrier).
+  __device__ __forceinline__ float *RawMatrix(unsigned set, unsigned i) const {
+    return raw_base + (3 * set + i) * static_cast<unsigned>(KP * KP);
+  }
+
+  __device__ __forceinline__ void Issue(unsigned set, const float *m0, const float *m1,
+                                        const float *m2, unsigned count) {
+    issued |= 1u << set;
+    if (threadIdx.x != 0)
+      return;
     const std::uint32_t bytes = KK * 4u;
-    if (threadIdx.x == 0) {
-      umma::FenceProxy();
-      umma::ExpectBytes(&sh.copy_barrier, bytes * count);
-      const float *sources[3] = {m0, m1, m2};
-      for (unsigned i = 0; i < count; ++i)
-        umma::BulkLoad(raw[i], sources[i], bytes, &sh.copy_barrier);
-    }
-    ok = umma::Wait(&sh.copy_barrier, copy_phase) && ok;
-    copy_phase ^= 1u;
+    umma::FenceProxy();
+    umma::ExpectBytes(&sh.copy_barrier[set], bytes * count);
+    umma::BulkLoad(RawMatrix(set, 0), m0, bytes, &sh.copy_barrier[set]);
+    if (count > 1)
+      umma::BulkLoad(RawMatrix(set, 1), m1, bytes, &sh.copy_barrier[set]);
+    if (count > 2)
+      umma::BulkLoad(RawMatrix(set, 2), m2, bytes, &sh.copy_barrier[set]);
+  }
+
+  // Makes raw set `set` current once its copies have landed (bounded wait;
+  // every thread calls it).
+  __device__ __forceinline__ void Await(unsigned set) {
+    ok = umma::Wait(&sh.copy_barrier[set], (copy_phase >> set) & 1u) && ok;
+    copy_phase ^= 1u << set;
+    issued &= ~(1u << set);
+    current = set;
+    raw[0] = RawMatrix(set, 0);
+    raw[1] = RawMatrix(set, 1);
+    raw[2] = RawMatrix(set, 2);
+  }
+
+  // The matrices of the current operation: taken from the copy issued ahead
+  // when there is one, else copied now; then the copy for the next operation
+  // of the same step (independent of this one) is started into the other set.
+  __device__ __forceinline__ void Fetch(const float *m0, const float *m1, const float *m2,
+                                        unsigned count, bool has_next, const float *n0,
+                                        const float *n1, const float *n2) {
+    const unsigned other = current ^ 1u;
+    const unsigned set = (issued >> other) & 1u ? other : current;
+    if (!((issued >> set) & 1u))
+      Issue(set, m0, m1, m2, count);
+    Await(set);
+    if (has_next)
+      Issue(set ^ 1u, n0, n1, n2, count);
   }
 
   // Row r of path version `ref` (input edge, or compressed path kFlag | t).
