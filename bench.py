@@ -1,6 +1,14 @@
 """Benchmark: batched posterior marginals (log Z + node/edge marginals, the
 gradient of log Z) over an uneven forest, on GB300.
 
+Workloads (--workload): `forest` (default, below); `gw`: Galton-Watson
+forest, K = 8, MAP + posterior sampling; `dense`: dense lognormal factors,
+spine-heavy trees at K = 64/128 on the tensor-core engine, or with --shape
+recursive --states 20 --tree-nodes 5000 the differentiation workload. Every
+workload autotunes the launch (thmm_autotune) before timing; the timed device
+steps replay a CUDA graph (thmm_enqueue); prepared calls overlap copies and
+kernels in stripes.
+
 Workload (one step = one categorical kFactors call over the whole forest):
 4096 trees with node counts log-uniform in [200, 20000], half random recursive
 trees, half caterpillars; K = 4 states (--states 20 for the larger variant);

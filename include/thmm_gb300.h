@@ -378,8 +378,8 @@ uint64_t thmm_workspace_launches(const thmm_workspace *workspace);
  * and log Z [batch]. Work is enqueued on `stream` (a cudaStream_t; NULL for
  * the default stream) and the call returns without waiting for it.
  *
- * Limits and sharing: a plan and batch whose program and scratch exceed the
- * static array are rejected with THMM_INVALID_ARGUMENT. The first call on a
+ * Limits and sharing: 1 to 32 states; a plan and batch whose program and
+ * scratch exceed the static array are rejected with THMM_INVALID_ARGUMENT. The first call on a
  * device resolves the array's device address (cudaGetSymbolAddress) and must
  * come before any stream capture. Every call reuses the same array, which keeps
  * the last call's contents; calls whose GPU work overlaps race, and the host
