@@ -39,6 +39,18 @@ struct ProgramSet {
                     bool categorical);
 };
 
+struct ProgramRequest {
+  const btrc::Plan *plan;
+  std::span<const std::uint32_t> observation_nodes;
+};
+
+// Programs of `requests`, in order, as one ProgramSet. Contiguous runs of
+// requests are compiled on up to `threads` host threads (0: all hardware
+// threads) into separate sets that are then concatenated with their array
+// offsets shifted, which gives exactly the arrays of a one-thread build.
+ProgramSet BuildPrograms(std::span<const ProgramRequest> requests, bool categorical,
+                         unsigned threads);
+
 // Kernel entry points. `kmax` is the padded state count (4, 8, 16, 20, 24
 // or 32; 64 or 128 for the wide-state engine).
 // With `blocks_per_sm` non-null the call only reports the occupancy. The

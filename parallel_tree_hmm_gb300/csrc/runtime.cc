@@ -337,9 +337,27 @@ struct Workspace {
   void Build(const std::vector<const btrc::Plan *> &instance_plans,
              const std::vector<std::vector<std::uint32_t>> &instance_observations,
              bool shared_edges) {
-    ProgramSet set;
     std::unordered_map<const btrc::Plan *, std::uint32_t> program_of;
     const std::size_t count = instance_plans.size();
+    // Which instances need a program of their own (a distinct plan, or a
+    // categorical forest tree with its own observation set), then all
+    // programs compiled on the host's threads.
+    std::vector<std::uint32_t> program_index(count);
+    std::vector<ProgramRequest> requests;
+    for (std::size_t i = 0; i < count; ++i) {
+      const btrc::Plan *p = instance_plans[i];
+      const auto found = program_of.find(p);
+      if (found != program_of.end() && (!categorical || shared_edges)) {
+        program_index[i] = found->second;
+        continue;
+      }
+      program_index[i] = static_cast<std::uint32_t>(requests.size());
+      program_of[p] = program_index[i];
+      requests.push_back({p, instance_observations.empty()
+                                 ? std::span<const std::uint32_t>()
+                                 : std::span<const std::uint32_t>(instance_observations[i])});
+    }
+    const ProgramSet set = BuildPrograms(requests, categorical, 0);
     std::vector<DevInstance> table(count);
     const std::uint64_t K = states;
     const std::uint64_t KK = K * K;
@@ -349,22 +367,8 @@ struct Workspace {
         std::max<std::size_t>(ScalarBytes(), compute_f64 ? 8 : 4);
     for (std::size_t i = 0; i < count; ++i) {
       const btrc::Plan &p = *instance_plans[i];
-      std::uint32_t program;
-      const auto found = program_of.find(&p);
-      if (found != program_of.end() && !categorical) {
-        program = found->second;
-      } else if (found != program_of.end() && shared_edges) {
-        program = found->second; // batch API: one plan, one observation set
-      } else {
-        program = set.Add(p, instance_observations.empty()
-                                 ? std::span<const std::uint32_t>()
-                                 : std::span<const std::uint32_t>(
-                                       instance_observations[i]),
-                          categorical);
-        program_of[&p] = program;
-      }
       DevInstance &instance = table[i];
-      instance.program = program;
+      instance.program = program_index[i];
       instance.node_base = node_base;
       instance.edge_in_base = shared_edges ? 0 : edge_base;
       instance.edge_out_base = edge_base;
