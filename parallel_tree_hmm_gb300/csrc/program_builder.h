@@ -152,6 +152,10 @@ std::uint32_t BuildProgram(const btrc::Plan &plan,
         out.gathers.push_back({g.parent | (stored[g.parent] ? 0u : kFlag),
                                slot[g.parent], g.first, g.count});
       }
+      // Each rake of the round is absorbed by exactly one gather: a second
+      // absorption batch after the same rake batch emits none, so a program
+      // never holds more gathers than rakes.
+      pending_count = 0;
       fused[fused_count++] = gather_step;
       for (const btrc::BranchAbsorption &op :
            plan.branch_absorptions().subspan(batch.offset, batch.count)) {

@@ -18,6 +18,13 @@
 // call's contents in it: calls whose GPU work overlaps (for example on two
 // streams) race, and the host side (a static host image) is not thread-safe.
 // Successive calls on one stream are ordered by that stream.
+//
+// The host image reaches the device by a copy from pageable host memory: the
+// CUDA runtime first waits for work already queued on the stream, then stages
+// the image before the call returns, so the next call may rebuild the image at
+// once. The sum-product forward kernel has no device-side failure mode (its
+// error word is never set); a zero partition shows up as log Z = -inf in the
+// caller's output.
 #include <cuda_runtime.h>
 
 #include <cstddef>
@@ -196,7 +203,9 @@ extern "C" thmm_status thmm_log_partition_static(
     Place(image, storage.absorbs, plan.branch_absorptions().size());
     Place(image, storage.compress, plan.num_compressions());
     Place(image, storage.compress_ends, plan.num_compressions());
-    Place(image, storage.gathers, plan.branch_absorptions().size());
+    // Every gather absorbs at least one rake, and each rake belongs to one
+    // gather (program_builder.h), so the rake count bounds the gathers.
+    Place(image, storage.gathers, plan.num_branches());
     BuildProgram(plan, {}, false, storage);
 
     DevInstance *instances = image.Take<DevInstance>(batch);
@@ -264,6 +273,7 @@ extern "C" thmm_status thmm_log_partition_static(
                                             std::max(setup.occupancy[index], 1))));
     Check(LaunchLinearF32(false, kmax, kLinearForward, args, grid, stream, nullptr),
           "tree-HMM accelerator kernel launch");
+    SetLastError("");
     return THMM_OK;
   } catch (const std::invalid_argument &error) {
     SetLastError(error.what());
