@@ -488,7 +488,7 @@ def run_ours(args, rank, world, local_rank, dist):
                 "api_upload_ms": [round(v, 3) for v in api_upload_ms],
                 "api_kernel_ms": [round(v, 3) for v in api_kernel_ms],
                 "api_download_ms": [round(v, 3) for v in api_download_ms],
-                "stripes": ws.launches // 2},
+                "launches_per_call": ws.launches},
         "gpu_launches": args.steps * launches_per_step,
         "clocks": sampler.summary(),
     }

@@ -335,14 +335,23 @@ thmm_status thmm_enqueue(thmm_workspace *workspace, int operation,
  * kernel k (0: forward sum-product sweep, 1: MAP, 2: sampling, 3: adjoint
  * sweep of the marginals); 0 means the occupancy limit. A prepared call is
  * cut into `stripes` (1 to 8; 0: one per 2 Mi nodes) contiguous runs of
- * instances whose input copies, kernels and output copies overlap. No
- * setting changes any result bit. */
+ * instances whose input copies, kernels and output copies overlap.
+ * `schedule` picks how sum-product calls (partition, log partition,
+ * marginals) are scheduled when the workspace has up to 4 states:
+ * THMM_SCHEDULE_TEAMS contracts each tree with one CTA or warp walking its
+ * plan step by step; THMM_SCHEDULE_PHASES runs each round of every tree in
+ * one grid-wide launch per operation kind (the default where available).
+ * Other workspaces always use THMM_SCHEDULE_TEAMS. No setting changes any
+ * result bit. */
+#define THMM_SCHEDULE_TEAMS 0
+#define THMM_SCHEDULE_PHASES 1
 typedef struct thmm_tuning {
   uint32_t team_threshold;
   uint32_t ctas_per_sm[4];
   uint32_t stripes;
   float kernel_ms;     /* device time per step of the chosen setting */
   uint32_t candidates; /* settings timed by the last autotune */
+  uint32_t schedule;   /* THMM_SCHEDULE_TEAMS or THMM_SCHEDULE_PHASES */
 } thmm_tuning;
 /* Times candidate settings for `operation` on the inputs left resident by a
  * prepared call (`repeats` timed steps each, after one untimed step), keeps
@@ -376,7 +385,18 @@ uint64_t thmm_workspace_launches(const thmm_workspace *workspace);
  * Inputs and outputs are the caller's device buffers, FP32: node factors
  * [batch, node, state], edge factors [edge, parent, child] shared by the batch,
  * and log Z [batch]. Work is enqueued on `stream` (a cudaStream_t; NULL for
- * the default stream) and the call returns without waiting for it.
+ * the default stream). The compiled plan reaches the device by an ordinary
+ * copy from host memory, so the call first waits for work already queued on
+ * `stream`; it returns once the plan is handed over, without waiting for the
+ * contraction itself.
+ *
+ * Results and errors: THMM_OK means the contraction was enqueued. It has no
+ * failure mode of its own on the device, so nothing is reported later. A tree
+ * whose partition is zero (every assignment has zero weight) gets log Z =
+ * -inf in `log_partitions`; unlike thmm_log_partition_function, which waits
+ * for the result and raises THMM_DOMAIN_ERROR, this call does not wait, so the
+ * caller checks the outputs. Argument errors return a status at once, with
+ * the message in thmm_last_error(), which a successful call clears.
  *
  * Limits and sharing: 1 to 32 states; a plan and batch whose program and
  * scratch exceed the static array are rejected with THMM_INVALID_ARGUMENT. The first call on a

@@ -40,6 +40,8 @@ THMM_OP_LOG_PARTITION = 1
 THMM_OP_MAXIMUM = 2
 THMM_OP_SAMPLE = 3
 THMM_OP_MARGINALS = 4
+THMM_SCHEDULE_TEAMS = 0
+THMM_SCHEDULE_PHASES = 1
 
 
 class PlanInfo(ctypes.Structure):
@@ -112,7 +114,8 @@ class MarginalResult(ctypes.Structure):
 
 class Tuning(ctypes.Structure):
     _fields_ = [("team_threshold", c_u32), ("ctas_per_sm", c_u32 * 4),
-                ("stripes", c_u32), ("kernel_ms", ctypes.c_float), ("candidates", c_u32)]
+                ("stripes", c_u32), ("kernel_ms", ctypes.c_float), ("candidates", c_u32),
+                ("schedule", c_u32)]
 
 
 # name -> (restype, argtypes)

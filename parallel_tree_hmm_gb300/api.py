@@ -512,12 +512,17 @@ class Workspace:
         return _tuning_dict(tuning)
 
     def set_tuning(self, team_threshold: int, ctas_per_sm=(0, 0, 0, 0),
-                   stripes: int = 0) -> None:
+                   stripes: int = 0, schedule: int | None = None) -> None:
+        """Applies a launch tuning. `schedule` (THMM_SCHEDULE_TEAMS or
+        THMM_SCHEDULE_PHASES) defaults to the workspace's current one."""
+        if schedule is None:
+            schedule = self.tuning["schedule"]
         tuning = _lib.Tuning()
         tuning.team_threshold = team_threshold
         for i, value in enumerate(ctas_per_sm):
             tuning.ctas_per_sm[i] = value
         tuning.stripes = stripes
+        tuning.schedule = schedule
         _check(self._lib.thmm_set_tuning(self._handle, ctypes.byref(tuning)))
 
     @property
@@ -536,7 +541,8 @@ def _tuning_dict(tuning) -> dict:
     return {"team_threshold": int(tuning.team_threshold),
             "ctas_per_sm": [int(v) for v in tuning.ctas_per_sm],
             "stripes": int(tuning.stripes),
-            "kernel_ms": float(tuning.kernel_ms), "candidates": int(tuning.candidates)}
+            "kernel_ms": float(tuning.kernel_ms), "candidates": int(tuning.candidates),
+            "schedule": int(tuning.schedule)}
 
 
 def available() -> bool:

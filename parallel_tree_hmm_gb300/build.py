@@ -53,6 +53,7 @@ SOURCES = [
     "engine_sample_f64.cu",
     "engine_sample_f32.cu",
     "engine_wide.cu",
+    "engine_phase.cu",
     "engine_linear_f32.cu",
     "engine_linear_f64.cu",
     "engine_maximum.cu",
@@ -60,6 +61,7 @@ SOURCES = [
     "static_scratch.cu",
     "runtime.cc",
     "program.cc",
+    "phase.cc",
     "btrc_plan.cc",
 ]
 
@@ -135,7 +137,8 @@ def build_oracle(reference: bool = True) -> None:
     is present, the reference CPU library and tests under oracle/_ref."""
     oracle_dir = ROOT / "oracle"
     subprocess.run(["make", "-s", "-C", str(oracle_dir)], check=True)
-    ref = os.environ.get("THMM_REFERENCE", "/root/reference")
+    # The reference checkout: $THMM_REFERENCE, else `reference` beside the repo.
+    ref = os.environ.get("THMM_REFERENCE", str(ROOT.parent / "reference"))
     if reference and os.path.isdir(os.path.join(ref, "src")):
         subprocess.run(["make", "-s", "-C", str(oracle_dir), "ref", f"REF={ref}"], check=True)
 

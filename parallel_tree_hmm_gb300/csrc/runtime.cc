@@ -34,6 +34,7 @@
 
 #include "btrc/plan.h"
 #include "engine.h"
+#include "phase.h"
 #include "program.h"
 
 struct thmm_plan; // a btrc::Plan in disguise
@@ -203,6 +204,19 @@ struct Workspace {
   std::vector<std::uint64_t> off_nodes, off_edges, off_obs;
   bool shared_edge_input = false;
 
+  // Level-synchronous phase schedule (phase.h) of the sum-product calls for
+  // up to 4 states; its node values and compressed paths live in `scratch`.
+  PhasePlan phase;
+  DeviceBuffer phase_rakes, phase_gathers, phase_compress, phase_roots;
+  DeviceBuffer node_exp, comp_exp;
+  std::uint32_t schedule = THMM_SCHEDULE_TEAMS;
+  // Operation ranges of each round for an instance range (cached).
+  struct PhaseRanges {
+    std::uint32_t a, b;
+    std::vector<std::pair<std::uint64_t, std::uint64_t>> gather, rake, compress;
+  };
+  std::vector<PhaseRanges> phase_ranges;
+
   // Device data.
   DeviceBuffer node_in, edge_in, observations, root_potential, emission;
   DeviceBuffer uniforms, values, node_out, edge_out, states_out, scratch, bytes;
@@ -235,10 +249,14 @@ struct Workspace {
     team_threshold = 0;
     std::fill(std::begin(cta_cap), std::end(cta_cap), 0);
     tuned_ms = 0.0f;
+    phase = PhasePlan{};
+    phase_ranges.clear();
+    schedule = THMM_SCHEDULE_TEAMS;
     for (DeviceBuffer *buffer :
          {&programs, &steps, &rakes, &combines, &absorbs, &compress, &instances,
           &compress_ends, &gathers, &team_order, &stripe_order, &control, &node_in,
-          &edge_in,
+          &phase_rakes, &phase_gathers, &phase_compress, &phase_roots, &node_exp,
+          &comp_exp, &edge_in,
           &observations, &root_potential, &emission, &uniforms, &values,
           &node_out, &edge_out, &states_out, &scratch, &bytes})
       buffer->Free();
@@ -433,6 +451,28 @@ struct Workspace {
     gathers.Upload(set.gathers, stream);
     instances.Upload(table, stream);
     team_order.Upload(order, stream);
+    // Phase schedule of the sum-product calls for up to 4 states.
+    if (PaddedStates(states) == 4) {
+      std::vector<PhaseInstance> phase_instances(count);
+      for (std::size_t i = 0; i < count; ++i)
+        phase_instances[i] = {table[i].program, table[i].node_base, table[i].edge_out_base,
+                              table[i].obs_base};
+      phase = BuildPhasePlan(set, phase_instances, total_nodes, total_edges_out, 0);
+      if (phase.enabled) {
+        phase_rakes.Upload(phase.rakes, stream);
+        phase_gathers.Upload(phase.gathers, stream);
+        phase_compress.Upload(phase.compress, stream);
+        phase_roots.Upload(phase.roots, stream);
+        node_exp.Allocate(total_nodes * sizeof(int));
+        comp_exp.Allocate(phase.total_compressions * sizeof(int));
+        // The records now live on the device; the host keeps the counts.
+        phase.rakes = {};
+        phase.gathers = {};
+        phase.compress = {};
+        phase.roots = {};
+        schedule = THMM_SCHEDULE_PHASES;
+      }
+    }
     // Work counters of the forward [0..1] and adjoint [4..5] launches; [2] is
     // the error word; words 8 + 8c .. 15 + 8c hold the counters of stripe c.
     control.Allocate((8 + 8 * kMaxStripes) * sizeof(std::uint32_t));
@@ -682,6 +722,85 @@ struct Workspace {
     return count;
   }
 
+  bool UsePhases(int operation) const {
+    return schedule == THMM_SCHEDULE_PHASES && phase.enabled &&
+           (operation == THMM_OP_PARTITION || operation == THMM_OP_LOG_PARTITION ||
+            operation == THMM_OP_MARGINALS);
+  }
+
+  const PhaseRanges &PhaseRangesFor(std::uint32_t a, std::uint32_t b) {
+    for (const PhaseRanges &ranges : phase_ranges)
+      if (ranges.a == a && ranges.b == b)
+        return ranges;
+    PhaseRanges ranges{a, b, {}, {}, {}};
+    for (std::uint32_t r = 0; r < phase.rounds; ++r) {
+      ranges.gather.push_back(phase.OpRange(kPhaseGather, r, a, b));
+      ranges.rake.push_back(phase.OpRange(kPhaseRakeReverse, r, a, b));
+      ranges.compress.push_back(phase.OpRange(kPhaseCompress, r, a, b));
+    }
+    if (phase_ranges.size() >= 32)
+      phase_ranges.erase(phase_ranges.begin());
+    phase_ranges.push_back(std::move(ranges));
+    return phase_ranges.back();
+  }
+
+  // Launches the phase schedule of `operation` over instances [a, b):
+  // gather and compress phases round by round, the finish phase, then (for
+  // marginals) the adjoint phases in reverse round order. Returns the number
+  // of kernel launches.
+  int LaunchPhases(int operation, std::uint32_t a, std::uint32_t b) {
+    const PhaseRanges &ranges = PhaseRangesFor(a, b);
+    const std::size_t K = states;
+    const std::size_t compute_bytes = compute_f64 ? 8 : 4;
+    unsigned char *work = scratch.as<unsigned char>();
+    PhaseArgs args{};
+    args.rakes = phase_rakes.as<uint4>();
+    args.gathers = phase_gathers.as<uint4>();
+    args.compress = phase_compress.as<uint4>();
+    args.roots = phase_roots.as<uint2>();
+    args.node_in = node_in.ptr;
+    args.observations = observations.as<std::uint8_t>();
+    args.root_potential = root_potential.ptr;
+    args.emission = emission.ptr;
+    args.categories = static_cast<std::uint32_t>(categories);
+    args.categorical = categorical ? 1u : 0u;
+    args.edge_in = edge_in.ptr;
+    args.edge_modulus = shared_edge_input ? static_cast<std::uint32_t>(edges_per_item) : 0u;
+    args.states = static_cast<std::uint32_t>(states);
+    args.nodes = work;
+    args.comps = work + total_nodes * K * compute_bytes;
+    args.comp_mu = work + (total_nodes * K + phase.total_compressions * K * K) * compute_bytes;
+    args.node_exp = node_exp.as<int>();
+    args.comp_exp = comp_exp.as<int>();
+    args.values = values.ptr;
+    args.node_out = node_out.ptr;
+    args.edge_out = edge_out.ptr;
+    args.raw = operation == THMM_OP_PARTITION ? 1u : 0u;
+    args.reverse = operation == THMM_OP_MARGINALS ? 1u : 0u;
+    int count = 0;
+    const auto launch = [&](int kind, std::pair<std::uint64_t, std::uint64_t> range) {
+      if (range.second <= range.first)
+        return;
+      args.offset = static_cast<std::uint32_t>(range.first);
+      args.count = static_cast<std::uint32_t>(range.second - range.first);
+      Check(LaunchPhase(scalar, compute_f64, kind, args, stream, nullptr),
+            "tree-HMM accelerator kernel launch");
+      ++count;
+    };
+    for (std::uint32_t r = 0; r < phase.rounds; ++r) {
+      launch(kPhaseGather, ranges.gather[r]);
+      launch(kPhaseCompress, ranges.compress[r]);
+    }
+    launch(kPhaseFinish, {a, b});
+    if (operation == THMM_OP_MARGINALS) {
+      for (std::uint32_t r = phase.rounds; r-- > 0;) {
+        launch(kPhaseCompressReverse, ranges.compress[r]);
+        launch(kPhaseRakeReverse, ranges.rake[r]);
+      }
+    }
+    return count;
+  }
+
   // One device step over all instances of the batch, on the workspace stream.
   void EnqueueDevice(int operation, std::size_t batch) {
     EngineArgs args = MakeArgs(operation);
@@ -695,8 +814,10 @@ struct Workspace {
       args.small_count = items_big ? 0u : static_cast<std::uint32_t>(batch);
     }
     Check(cudaMemsetAsync(control.ptr, 0, 32, stream), "cudaMemsetAsync");
+    const auto items = static_cast<std::uint32_t>(forest ? capacity : batch);
     launches = static_cast<std::uint64_t>(
-        LaunchTeams(operation, args, control.as<std::uint32_t>()));
+        UsePhases(operation) ? LaunchPhases(operation, 0, items)
+                             : LaunchTeams(operation, args, control.as<std::uint32_t>()));
   }
 
   // Splits the largest-first queue at `threshold` nodes (CTA teams above).
@@ -786,6 +907,7 @@ struct Workspace {
     };
     const std::vector<int> forward_caps = caps_for(slot);
     const std::vector<int> reverse_caps = adjoint ? caps_for(3) : std::vector<int>{0};
+    schedule = THMM_SCHEDULE_TEAMS; // team candidates first
     thmm_tuning best{};
     best.kernel_ms = std::numeric_limits<float>::infinity();
     std::uint32_t tried = 0;
@@ -807,6 +929,16 @@ struct Workspace {
         }
       }
     }
+    // The phase schedule has no team or occupancy setting of its own.
+    if (phase.enabled && operation != THMM_OP_MAXIMUM && operation != THMM_OP_SAMPLE) {
+      schedule = THMM_SCHEDULE_PHASES;
+      const float ms = TimeSteps(operation, repeats);
+      ++tried;
+      if (ms < best.kernel_ms) {
+        best.kernel_ms = ms;
+        best.schedule = THMM_SCHEDULE_PHASES;
+      }
+    }
     best.candidates = tried;
     best.stripes = stripes_setting;
     ApplyTuning(best);
@@ -814,6 +946,9 @@ struct Workspace {
   }
 
   void ApplyTuning(const thmm_tuning &tuning) {
+    if (tuning.schedule != THMM_SCHEDULE_TEAMS && tuning.schedule != THMM_SCHEDULE_PHASES)
+      throw std::invalid_argument("unknown schedule");
+    schedule = phase.enabled ? tuning.schedule : THMM_SCHEDULE_TEAMS;
     ApplyThreshold(tuning.team_threshold);
     for (int slot = 0; slot < 4; ++slot)
       cta_cap[slot] = static_cast<int>(tuning.ctas_per_sm[slot]);
@@ -828,6 +963,7 @@ struct Workspace {
       tuning.ctas_per_sm[slot] = static_cast<std::uint32_t>(cta_cap[slot]);
     tuning.stripes = stripes_setting;
     tuning.kernel_ms = tuned_ms;
+    tuning.schedule = schedule;
     return tuning;
   }
 
@@ -1000,7 +1136,9 @@ struct Workspace {
       args.small_items = stripe_order.as<std::uint32_t>() + stripe.first + stripe.big;
       args.small_count = stripe.small;
       count += static_cast<std::uint64_t>(
-          LaunchTeams(operation, args, control.as<std::uint32_t>() + 8 + 8 * c));
+          UsePhases(operation)
+              ? LaunchPhases(operation, stripe.first, stripe.last)
+              : LaunchTeams(operation, args, control.as<std::uint32_t>() + 8 + 8 * c));
       Check(cudaEventRecord(computed[c], stream), "cudaEventRecord");
     }
     Check(cudaEventRecord(t[3], stream), "cudaEventRecord");

@@ -303,7 +303,13 @@ def test_enqueue_matches_prepared_call(gpu):
     first = ws.posterior_marginals_prepared(
         gpu.BatchedModelView(plan, states, batch, nodes.ravel(), edges))
     values = first.log_partitions.copy()
-    assert ws.launches == 2  # forward sweep, then adjoint sweep
+    # Phase schedule (the default at K <= 4): gather and compress launches per
+    # round, the finish launch, two adjoint launches per round.
+    assert plan.num_rounds * 2 + 1 <= ws.launches <= plan.num_rounds * 4 + 1
+    ws.set_tuning(1024, schedule=0)
+    ws.posterior_marginals_prepared(
+        gpu.BatchedModelView(plan, states, batch, nodes.ravel(), edges))
+    assert ws.launches == 2  # per-tree teams: forward sweep, then adjoint sweep
     assert ws.enqueue(4) == batch * plan.num_nodes
     ws.synchronize()
     again = ws.posterior_marginals_prepared(

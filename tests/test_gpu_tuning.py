@@ -1,16 +1,23 @@
-"""Launch tuning and graph replay change no result bit.
+"""Launch tuning, schedules and graph replay change no result bit.
 
 The team threshold (which trees a whole CTA contracts instead of one warp),
 the CTAs per SM of each kernel and CUDA-graph replay of the device-only step
-only move work between SMs, CTAs and warps; every operation's arithmetic and
-the integer exponent sums are the same, so every output must be bit-identical.
+only move work between SMs, CTAs and warps; the phase schedule (every round
+of every tree in one grid-wide launch, K <= 4) performs each operation's
+arithmetic in the same order and carries the power-of-two exponents with the
+stored values instead of per team. Every operation's floating-point result
+and the integer exponent sums are the same, so every output must be
+bit-identical across all of them.
 """
 import numpy as np
 import pytest
 
-from parallel_tree_hmm_gb300 import synthetic
+from parallel_tree_hmm_gb300 import _lib, synthetic
 
 pytestmark = pytest.mark.gpu
+
+TEAMS = _lib.THMM_SCHEDULE_TEAMS
+PHASES = _lib.THMM_SCHEDULE_PHASES
 
 
 def forest(gpu, rng, states):
@@ -35,18 +42,24 @@ def test_tunings_give_identical_marginals(gpu, states):
     ws = gpu.Workspace()
     ws.reserve_forest(plans, states, kind="marginals", scalar=np.float32)
     model = gpu.BatchedModelView(None, states, len(plans), nodes, edges)
+    # The phase schedule exists for up to 4 states and is then the default.
+    assert ws.tuning["schedule"] == (PHASES if states <= 4 else TEAMS)
     reference = outputs(ws.posterior_marginals_prepared(model))
     settings = [(1, (0, 0, 0, 0)),          # every tree to a CTA team
                 (1 << 31, (0, 0, 0, 0)),    # every tree to a warp team
                 (1000, (1, 0, 0, 1)),       # one CTA per SM for both sweeps
                 (300, (2, 0, 0, 3))]
-    for threshold, caps in settings:
-        ws.set_tuning(threshold, caps)
-        assert ws.tuning["team_threshold"] == threshold
-        assert ws.tuning["ctas_per_sm"] == list(caps)
-        got = outputs(ws.posterior_marginals_prepared(model))
-        for a, b in zip(got, reference):
-            assert np.array_equal(a, b)
+    for schedule in (TEAMS, PHASES):
+        for threshold, caps in settings:
+            ws.set_tuning(threshold, caps, schedule=schedule)
+            assert ws.tuning["team_threshold"] == threshold
+            assert ws.tuning["ctas_per_sm"] == list(caps)
+            assert ws.tuning["schedule"] == (schedule if states <= 4 else TEAMS)
+            got = outputs(ws.posterior_marginals_prepared(model))
+            for a, b in zip(got, reference):
+                assert np.array_equal(a, b)
+            log_z = np.array(ws.log_partition_function_prepared(model).values)
+            assert np.array_equal(log_z, reference[0])
     chosen = ws.autotune(4, repeats=1)
     assert chosen["candidates"] >= 2 and chosen["kernel_ms"] > 0
     assert ws.tuning["team_threshold"] == chosen["team_threshold"]
@@ -55,11 +68,13 @@ def test_tunings_give_identical_marginals(gpu, states):
         assert np.array_equal(a, b)
 
 
-def test_graph_replay_matches_prepared_call(gpu):
+@pytest.mark.parametrize("schedule", [TEAMS, PHASES])
+def test_graph_replay_matches_prepared_call(gpu, schedule):
     rng = np.random.default_rng(77)
     plans, nodes, edges = forest(gpu, rng, 4)
     ws = gpu.Workspace()
     ws.reserve_forest(plans, 4, kind="marginals", scalar=np.float32)
+    ws.set_tuning(1024, schedule=schedule)
     model = gpu.BatchedModelView(None, 4, len(plans), nodes, edges)
     reference = outputs(ws.posterior_marginals_prepared(model))
     staged = ws.inputs()
@@ -67,7 +82,11 @@ def test_graph_replay_matches_prepared_call(gpu):
     for _ in range(3):  # capture, then two replays
         assert ws.enqueue(4) == total
     ws.synchronize()
-    assert ws.launches == 2
+    if schedule == TEAMS:
+        assert ws.launches == 2
+    else:  # gather + compress per round, finish, two adjoint phases per round
+        rounds = max(p.num_rounds for p in plans)
+        assert 2 * rounds + 1 <= ws.launches <= 4 * rounds + 1
     # Outputs of the replays are in device memory; a kNone-style rerun through
     # the prepared call downloads the same values.
     got = outputs(ws.posterior_marginals_prepared(
@@ -114,17 +133,20 @@ def test_striped_calls_match_single_stripe(gpu):
     ws = gpu.Workspace()
     ws.reserve_forest(plans, 4, kind="marginals", scalar=np.float32)
     model = gpu.BatchedModelView(None, 4, len(plans), nodes, edges)
-    ws.set_tuning(1024, stripes=1)
+    ws.set_tuning(1024, stripes=1, schedule=TEAMS)
     single = outputs(ws.posterior_marginals_prepared(model))
     single_log_z = np.array(ws.log_partition_function_prepared(model).values)
-    for stripes in (2, 3, 8):
-        ws.set_tuning(1024, stripes=stripes)
-        assert ws.tuning["stripes"] == stripes
-        for a, b in zip(outputs(ws.posterior_marginals_prepared(model)), single):
-            assert np.array_equal(a, b)
-        # Stripes balance nodes, so a dominant tree can merge stripes.
-        assert ws.launches % 2 == 0 and 2 <= ws.launches <= 2 * stripes
-        assert np.array_equal(ws.log_partition_function_prepared(model).values, single_log_z)
+    for schedule in (TEAMS, PHASES):
+        for stripes in (2, 3, 8):
+            ws.set_tuning(1024, stripes=stripes, schedule=schedule)
+            assert ws.tuning["stripes"] == stripes
+            for a, b in zip(outputs(ws.posterior_marginals_prepared(model)), single):
+                assert np.array_equal(a, b)
+            # Stripes balance nodes, so a dominant tree can merge stripes.
+            if schedule == TEAMS:
+                assert ws.launches % 2 == 0 and 2 <= ws.launches <= 2 * stripes
+            assert np.array_equal(ws.log_partition_function_prepared(model).values,
+                                  single_log_z)
 
     ws2 = gpu.Workspace()
     ws2.reserve_forest(plans, 4, kind="maximum,sampling", scalar=np.float32)
@@ -152,12 +174,14 @@ def test_striped_categorical_and_batch_api(gpu):
     staged.emission_potentials[:] = rng.random(K * K) + 0.1
     staged.edge_potentials[:] = rng.random(staged.edge_potentials.size) + 0.1
     staged.observations[:] = rng.integers(0, K, staged.observations.size)
-    ws.set_tuning(1024, stripes=1)
+    ws.set_tuning(1024, stripes=1, schedule=TEAMS)
     single = outputs(ws.posterior_marginals_prepared(staged, 0))  # kAll
-    ws.set_tuning(1024, stripes=3)
-    for update in (0, 1, 2):  # kAll, kFactors, kNone
-        for a, b in zip(outputs(ws.posterior_marginals_prepared(staged, update)), single):
-            assert np.array_equal(a, b)
+    for schedule in (TEAMS, PHASES):
+        ws.set_tuning(1024, stripes=3, schedule=schedule)
+        for update in (0, 1, 2):  # kAll, kFactors, kNone
+            for a, b in zip(outputs(ws.posterior_marginals_prepared(staged, update)),
+                            single):
+                assert np.array_equal(a, b)
 
     plan = gpu.Plan(synthetic.random_recursive(rng, 600))
     batch = 7
@@ -166,15 +190,18 @@ def test_striped_categorical_and_batch_api(gpu):
     wb = gpu.Workspace()
     wb.reserve_marginals(plan, K, batch, scalar=np.float32)
     view = gpu.BatchedModelView(plan, K, batch, dense_nodes, dense_edges)
-    wb.set_tuning(1024, stripes=1)
+    wb.set_tuning(1024, stripes=1, schedule=TEAMS)
     single = outputs(wb.posterior_marginals_prepared(view))
-    wb.set_tuning(1024, stripes=4)
-    for a, b in zip(outputs(wb.posterior_marginals_prepared(view)), single):
-        assert np.array_equal(a, b)
+    for schedule in (TEAMS, PHASES):
+        wb.set_tuning(1024, stripes=4, schedule=schedule)
+        for a, b in zip(outputs(wb.posterior_marginals_prepared(view)), single):
+            assert np.array_equal(a, b)
     small = gpu.BatchedModelView(plan, K, 3, dense_nodes[:3 * plan.num_nodes * K],
                                  dense_edges)
-    wb.set_tuning(1024, stripes=1)
+    wb.set_tuning(1024, stripes=1, schedule=TEAMS)
     single = outputs(wb.posterior_marginals_prepared(small))
-    wb.set_tuning(1024, stripes=4)
-    for a, b in zip(outputs(wb.posterior_marginals_prepared(small)), single):
-        assert np.array_equal(a, b)
+    for schedule in (TEAMS, PHASES):
+        for stripes in (1, 4):
+            wb.set_tuning(1024, stripes=stripes, schedule=schedule)
+            for a, b in zip(outputs(wb.posterior_marginals_prepared(small)), single):
+                assert np.array_equal(a, b)
