@@ -68,6 +68,8 @@ def parse_args():
     parser.add_argument("--seed", type=int, default=0)
     parser.add_argument("--e2e-steps", type=int, default=None)
     parser.add_argument("--cpu-sample-nodes", type=int, default=20_000_000)
+    parser.add_argument("--check-trees", type=int, default=16,
+                        help="gw workload: trees checked against the oracle")
     parser.add_argument("--workload", choices=["forest", "gw", "dense"], default="forest",
                         help="forest: uneven forest, marginals (default); gw: "
                              "Galton-Watson forest, MAP + posterior sampling; dense: "
@@ -117,6 +119,7 @@ class Forest:
         self.total_edges = int((self.num_nodes - 1).sum())
         self.total_observed = int(sum(len(o) for o in self.observed))
         self.rng = rng
+        self.cpu_plans = {}  # tree -> oracle planner plan (CPU legs)
 
     def factors(self, seed: int):
         """One kFactors draw: root, emission and edge factors (float32)."""
@@ -210,8 +213,9 @@ class ClockSampler:
 # ---------------------------------------------------------------- CPU leg
 def cpu_baseline(forest: Forest, root, emission, edges, observations, sample_nodes):
     """Reference FP64 CPU marginals (oracle port) on the first trees of the
-    forest whose node count reaches `sample_nodes`, over all host cores."""
-    import parallel_tree_hmm_gb300 as thmm
+    forest whose node count reaches `sample_nodes`, over all host cores. Plans
+    come from the oracle's own planner library, so this leg loads no product
+    code."""
     from oracle import bridge
 
     K = forest.states
@@ -233,7 +237,9 @@ def cpu_baseline(forest: Forest, root, emission, edges, observations, sample_nod
         obs = observations[obs_offsets[t]:obs_offsets[t + 1]]
         dense[forest.observed[t]] *= emission64[obs]
         tree_edges = edges[edge_offsets[t] * K * K:edge_offsets[t + 1] * K * K]
-        jobs.append((thmm.Plan(parents), dense.ravel(), tree_edges.astype(np.float64)))
+        if t not in forest.cpu_plans:
+            forest.cpu_plans[t] = bridge.CpuPlan(parents)
+        jobs.append((forest.cpu_plans[t], dense.ravel(), tree_edges.astype(np.float64)))
     cores = os.cpu_count() or 1
 
     def run(job):
@@ -301,9 +307,11 @@ def run_reference(args, rank, world, dist):
     forest = Forest(args.trees, args.states, args.seed)
     root, emission, edges = forest.factors(args.seed + 1)
     observations = forest.observations()
-    sample = max(200_000, args.cpu_sample_nodes // 4)
+    # Every step contracts the whole forest (the same workload as the GPU
+    # arm), about a second on the GPU host's cores.
+    sample = forest.total_nodes
     for _ in range(args.warmup):
-        cpu_baseline(forest, root, emission, edges, observations, sample // 4)
+        cpu_baseline(forest, root, emission, edges, observations, sample // 8)
     values = []
     for _ in range(args.steps):
         values.append(cpu_baseline(forest, root, emission, edges, observations, sample))
@@ -573,7 +581,7 @@ def run_gw(args, rank, world, local_rank, dist):
         for _ in range(args.warmup + args.steps):
             start = time.perf_counter()
             nodes = 0
-            jobs = [(t, thmm.Plan(forest.parents[t])) for t in range(sample_trees)]
+            jobs = [(t, bridge.CpuPlan(forest.parents[t])) for t in range(sample_trees)]
 
             def run(job):
                 t, plan = job
@@ -619,24 +627,45 @@ def run_gw(args, rank, world, local_rank, dist):
     sample_states = np.array(ws.posterior_sample_prepared(
         staged, uniforms, thmm.CategoricalInputUpdate.kNone).states)
 
-    # Bit-exact check on the first trees against the oracle (FP32, reproducible
-    # exp/log) and agreement of the MAP states with the FP64 oracle.
-    check_trees = min(8, args.trees)
-    exact, agree, checked = 0, 0, 0
+    # Checks on the first trees (the oracle as checker):
+    #  * bit-exactness against the oracle with the device's reproducible
+    #    exp/log (FP32);
+    #  * agreement of MAP states and samples with the reference FP32 build
+    #    (libm-mode oracle) and with FP64, every disagreement classified by the
+    #    margin of the comparison that decided it (oracle/agreement.py).
+    from oracle import agreement
+
+    check_trees = min(args.check_trees, args.trees)
+    exact = 0
+    parts = {"map_fp32_reference": [], "sample_fp32_reference": [], "map_fp64": [],
+             "sample_fp64": []}
     node0 = 0
     for t in range(check_trees):
         n = int(forest.num_nodes[t])
+        got_map, got_sample = map_states[node0:node0 + n], sample_states[node0:node0 + n]
         dense, edges, u = forest.tree_inputs(t, np.float32)
-        w32, s32 = bridge.maximum(plans[t], K, dense, edges, np.float32, bridge.MATH_PORTABLE)
-        draw = bridge.sample(plans[t], K, dense, edges, u, np.float32, bridge.MATH_PORTABLE)
-        exact += int(np.array_equal(s32, map_states[node0:node0 + n]) and
-                     w32 == map_weights[t] and
-                     np.array_equal(draw, sample_states[node0:node0 + n]))
+        if t < 8:
+            w32, s32 = bridge.maximum(plans[t], K, dense, edges, np.float32,
+                                      bridge.MATH_PORTABLE)
+            draw = bridge.sample(plans[t], K, dense, edges, u, np.float32,
+                                 bridge.MATH_PORTABLE)
+            exact += int(np.array_equal(s32, got_map) and w32 == map_weights[t] and
+                         np.array_equal(draw, got_sample))
+        _, s, m = bridge.maximum_margins(plans[t], K, dense, edges, np.float32)
+        parts["map_fp32_reference"].append(
+            agreement.classify(plans[t], got_map, s, m, agreement.MAP_TIE_MARGIN))
+        s, m = bridge.sample_margins(plans[t], K, dense, edges, u, np.float32)
+        parts["sample_fp32_reference"].append(
+            agreement.classify(plans[t], got_sample, s, m, agreement.SAMPLE_TIE_MARGIN))
         dense64, edges64, _ = forest.tree_inputs(t, np.float64)
-        _, s64 = bridge.maximum(plans[t], K, dense64, edges64)
-        agree += int(np.sum(s64 == map_states[node0:node0 + n]))
-        checked += n
+        _, s, m = bridge.maximum_margins(plans[t], K, dense64, edges64)
+        parts["map_fp64"].append(
+            agreement.classify(plans[t], got_map, s, m, agreement.MAP_TIE_MARGIN))
+        s, m = bridge.sample_margins(plans[t], K, dense64, edges64, u.astype(np.float64))
+        parts["sample_fp64"].append(
+            agreement.classify(plans[t], got_sample, s, m, agreement.SAMPLE_TIE_MARGIN))
         node0 += n
+    agreements = {key: agreement.merge(value) for key, value in parts.items()}
 
     tuning_map = ws.autotune(2, repeats=2)
     tuning_sample = ws.autotune(3, repeats=2)
@@ -689,8 +718,14 @@ def run_gw(args, rank, world, local_rank, dist):
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f32", "data": "synthetic",
         "config": {**config, "tuning_map": tuning_map, "tuning_sample": tuning_sample,
-                   "bit_exact_trees": f"{exact}/{check_trees}",
-                   "map_fp64_state_agreement": agree / checked},
+                   "bit_exact_trees": f"{exact}/{min(8, check_trees)}",
+                   "agreement_trees": check_trees,
+                   "map_fp32_reference_agreement": agreements["map_fp32_reference"]["rate"],
+                   "sample_fp32_reference_agreement":
+                       agreements["sample_fp32_reference"]["rate"],
+                   "map_fp64_agreement": agreements["map_fp64"]["rate"],
+                   "sample_fp64_agreement": agreements["sample_fp64"]["rate"],
+                   "agreement_detail": agreements},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak,
                      "peak_source": "measured" if peaks else "fallback",
@@ -700,6 +735,27 @@ def run_gw(args, rank, world, local_rank, dist):
         "gpu_launches": 2 * args.steps,
         "clocks": sampler.summary(),
     }
+    if rank == 0 and world == 1 and args.cpu_sample_nodes > 0:
+        # Reference FP64 CPU MAP + sample (oracle port) on the first trees,
+        # over all host cores; plans from the oracle's planner library.
+        sample_trees = max(1, min(args.trees, 64))
+        jobs = [(t, bridge.CpuPlan(forest.parents[t])) for t in range(sample_trees)]
+
+        def run_cpu(job):
+            t, plan = job
+            dense, edges, u = forest.tree_inputs(t, np.float64)
+            bridge.maximum(plan, K, dense, edges)
+            bridge.sample(plan, K, dense, edges, u.astype(np.float64))
+            return plan.num_nodes
+
+        start = time.perf_counter()
+        with concurrent.futures.ThreadPoolExecutor(os.cpu_count() or 1) as pool:
+            done = sum(pool.map(run_cpu, jobs))
+        elapsed = time.perf_counter() - start
+        line["cpu_baseline"] = {"value": done / elapsed, "unit": UNIT,
+                                "cores": os.cpu_count() or 1, "kind": "port",
+                                "sample": f"first {sample_trees} trees ({done} nodes), "
+                                          f"FP64 MAP + sample, {elapsed:.2f} s"}
     if rank == 0:
         print(json.dumps(line), flush=True)
 
@@ -722,7 +778,10 @@ def run_dense(args, rank, world, local_rank, dist):
     rng = np.random.default_rng(rank_seed(args.seed, rank))
     grow = synthetic.spine_heavy if args.shape == "spine-heavy" else synthetic.random_recursive
     parents = [grow(rng, args.tree_nodes) for _ in range(args.trees)]
-    plans = thmm.Plan.many(parents)
+    # The reference arm plans with the oracle's planner library (no product
+    # code loaded); the same planner source gives the same plans.
+    plans = ([bridge.CpuPlan(p) for p in parents] if args.impl == "reference"
+             else thmm.Plan.many(parents))
     total_nodes = sum(p.num_nodes for p in plans)
     total_edges = sum(p.num_edges for p in plans)
     compressions = sum(int(p.num_compressions) for p in plans)

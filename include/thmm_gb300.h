@@ -368,6 +368,16 @@ thmm_status thmm_workspace_synchronize(thmm_workspace *workspace);
 /* Kernel launches made by the most recent prepared call or enqueue. */
 uint64_t thmm_workspace_launches(const thmm_workspace *workspace);
 
+/* Diagnostic (no reference counterpart): exercises the error path of the
+ * tensor-core engine's bounded waits on `device`. One warp takes tensor
+ * memory, waits on an mbarrier whose phase cannot complete (bulk-copy bytes
+ * announced, no copy issued) for at most `cycles` SM cycles, records the
+ * timeout exactly as the wide-state kernels do and releases the tensor
+ * memory. The host then reports the recorded timeout as the prepared calls
+ * do: THMM_RUNTIME_ERROR with the same message. THMM_OK would mean the wait
+ * did not give up. Nothing else on the device is affected. */
+thmm_status thmm_wait_timeout_check(int device, uint64_t cycles);
+
 /* ---------------------------------------------------- allocation-free path */
 /* Size of the device array that holds every intermediate of
  * thmm_log_partition_static. */

@@ -47,8 +47,79 @@ def _u32(array) -> ctypes.POINTER(ctypes.c_uint32):
     return array.ctypes.data_as(ctypes.POINTER(ctypes.c_uint32))
 
 
+PLAN_LIB = HERE / "liboracle_plan.so"
+_PLANNER = None
+
+
+def planner() -> ctypes.CDLL:
+    """liboracle_plan.so: the restated planner for the CPU baselines."""
+    global _PLANNER
+    if _PLANNER is None:
+        if not PLAN_LIB.exists():
+            subprocess.run(["make", "-s", "-C", str(HERE)], check=True)
+        lib = ctypes.CDLL(str(PLAN_LIB))
+        lib.oracle_plan_create.argtypes = [ctypes.POINTER(ctypes.c_int64), ctypes.c_size_t]
+        lib.oracle_plan_create.restype = ctypes.c_void_p
+        lib.oracle_plan_destroy.argtypes = [ctypes.c_void_p]
+        lib.oracle_plan_destroy.restype = None
+        lib.oracle_plan_view.argtypes = [ctypes.c_void_p, ctypes.POINTER(OraclePlan)]
+        lib.oracle_plan_view.restype = None
+        _PLANNER = lib
+    return _PLANNER
+
+
+class CpuPlan:
+    """A tree's rake/compress plan built by liboracle_plan.so, with the
+    attributes the oracle functions read (those of
+    parallel_tree_hmm_gb300.Plan), so CPU baselines need no product library."""
+
+    def __init__(self, parents):
+        parents = np.ascontiguousarray(parents, dtype=np.int64)
+        self._lib = planner()
+        self._handle = self._lib.oracle_plan_create(
+            parents.ctypes.data_as(ctypes.POINTER(ctypes.c_int64)), parents.size)
+        if not self._handle:
+            raise ValueError("not a tree")
+        view = OraclePlan()
+        self._lib.oracle_plan_view(self._handle, ctypes.byref(view))
+        self._view = view
+        self.num_nodes = view.num_nodes
+        self.num_edges = view.num_edges
+        self.root = view.root
+        self.num_branches = view.num_rakes
+        self.num_combinations = view.num_combinations
+        self.num_absorptions = view.num_absorptions
+        self.num_compressions = view.num_compressions
+        self.num_batches = view.num_batches
+
+    def _array(self, pointer, rows, width):
+        if rows == 0:
+            return np.zeros((0, width), dtype=np.uint32)
+        return np.ctypeslib.as_array(pointer, shape=(rows * width,)).reshape(rows, width).copy()
+
+    @property
+    def rakes(self):
+        return self._array(self._view.rakes, self.num_branches, 4)
+
+    @property
+    def compressions(self):
+        return self._array(self._view.compressions, self.num_compressions, 6)
+
+    def __del__(self):
+        handle = getattr(self, "_handle", None)
+        if handle:
+            self._lib.oracle_plan_destroy(handle)
+            self._handle = None
+
+
 def oracle_plan(plan):
-    """OraclePlan struct for a parallel_tree_hmm_gb300.Plan (keeps arrays alive)."""
+    """OraclePlan struct for a parallel_tree_hmm_gb300.Plan or a CpuPlan
+    (keeps the arrays alive)."""
+    if isinstance(plan, CpuPlan):
+        struct = OraclePlan()
+        ctypes.pointer(struct)[0] = plan._view
+        struct._keep = plan
+        return struct
     keep = [np.ascontiguousarray(a, dtype=np.uint32) for a in (
         plan.edge_parents, plan.edge_children, plan.rakes, plan.combinations,
         plan.absorptions, plan.compressions, plan.batches)]
@@ -79,6 +150,8 @@ def library() -> ctypes.CDLL:
                 f"oracle_marginals_{name}": [plan, size, p, p, p, p, p, p],
                 f"oracle_map_{name}": [plan, size, p, p, ctypes.c_int, p, u],
                 f"oracle_sample_{name}": [plan, size, p, p, p, ctypes.c_int, u],
+                f"oracle_map_margins_{name}": [plan, size, p, p, ctypes.c_int, p, u, p],
+                f"oracle_sample_margins_{name}": [plan, size, p, p, p, ctypes.c_int, u, p],
             }
             for fn, args in sig.items():
                 getattr(_ORACLE, fn).argtypes = args
@@ -148,6 +221,37 @@ def maximum(plan, states, nodes, edges, dtype=np.float64, math=MATH_LIBM):
         ctypes.byref(oracle_plan(plan)), states, _ptr(nodes), _ptr(edges), math,
         _ptr(weight), _u32(assignment)))
     return weight[0], assignment
+
+
+def maximum_margins(plan, states, nodes, edges, dtype=np.float64, math=MATH_LIBM):
+    """(log weight, states [N] uint32, margins [N]): MAP with, per node, the
+    gap between the chosen maximum and the best other candidate of the
+    comparison that decided its state."""
+    nodes = np.ascontiguousarray(nodes, dtype=dtype)
+    edges = np.ascontiguousarray(edges, dtype=dtype)
+    weight = np.zeros(1, dtype=dtype)
+    assignment = np.zeros(plan.num_nodes, dtype=np.uint32)
+    margins = np.zeros(plan.num_nodes, dtype=dtype)
+    _check(getattr(library(), f"oracle_map_margins_{_suffix(dtype)}")(
+        ctypes.byref(oracle_plan(plan)), states, _ptr(nodes), _ptr(edges), math,
+        _ptr(weight), _u32(assignment), _ptr(margins)))
+    return weight[0], assignment, margins
+
+
+def sample_margins(plan, states, nodes, edges, uniforms, dtype=np.float64,
+                   math=MATH_LIBM):
+    """(states [N] uint32, margins [N]): a posterior sample with, per node,
+    the distance from its uniform to the nearer end of the chosen state's
+    cumulative interval."""
+    nodes = np.ascontiguousarray(nodes, dtype=dtype)
+    edges = np.ascontiguousarray(edges, dtype=dtype)
+    uniforms = np.ascontiguousarray(uniforms, dtype=dtype)
+    assignment = np.zeros(plan.num_nodes, dtype=np.uint32)
+    margins = np.zeros(plan.num_nodes, dtype=dtype)
+    _check(getattr(library(), f"oracle_sample_margins_{_suffix(dtype)}")(
+        ctypes.byref(oracle_plan(plan)), states, _ptr(nodes), _ptr(edges),
+        _ptr(uniforms), math, _u32(assignment), _ptr(margins)))
+    return assignment, margins
 
 
 def sample(plan, states, nodes, edges, uniforms, dtype=np.float64, math=MATH_LIBM):

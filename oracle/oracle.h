@@ -95,6 +95,28 @@ int oracle_sample_f32(const oracle_plan *plan, size_t states,
                       const float *nodes, const float *edges,
                       const float *uniforms, int math, uint32_t *assignment);
 
+/* The same MAP and sample with, for every node, the margin of the
+ * comparison that decided its state (diagnostic, for classifying
+ * disagreements between two implementations): for MAP the gap between the
+ * chosen maximum and the best other candidate of its choice, relative to
+ * max(1, |maximum|); for sampling
+ * the distance from the node's uniform to the nearer end of the chosen
+ * state's cumulative interval. */
+int oracle_map_margins_f64(const oracle_plan *plan, size_t states, const double *nodes,
+                           const double *edges, int math, double *log_weight,
+                           uint32_t *assignment, double *margins);
+int oracle_map_margins_f32(const oracle_plan *plan, size_t states, const float *nodes,
+                           const float *edges, int math, float *log_weight,
+                           uint32_t *assignment, float *margins);
+int oracle_sample_margins_f64(const oracle_plan *plan, size_t states,
+                              const double *nodes, const double *edges,
+                              const double *uniforms, int math, uint32_t *assignment,
+                              double *margins);
+int oracle_sample_margins_f32(const oracle_plan *plan, size_t states,
+                              const float *nodes, const float *edges,
+                              const float *uniforms, int math, uint32_t *assignment,
+                              float *margins);
+
 /* Portable exp/log exposed for the error-bound tests. */
 float oracle_portable_expf(float x);
 float oracle_portable_logf(float x);

@@ -26,6 +26,8 @@ typedef struct {
   S *scratch;
   uint32_t *rake_choices;
   uint32_t *compression_choices;
+  S *rake_margins;        /* optional: runner-up gap of every rake choice */
+  S *compression_margins; /* optional: same for every compression choice */
   uint32_t *assignment;
   S log_partition;
   S max_log_weight;
@@ -50,6 +52,8 @@ static void SFX(store_free)(SFX(store) * st) {
   free(st->scratch);
   free(st->rake_choices);
   free(st->compression_choices);
+  free(st->rake_margins);
+  free(st->compression_margins);
 }
 
 static S *SFX(zeros)(size_t count) {
@@ -141,23 +145,6 @@ static S SFX(log_sum_exp)(size_t size, const S *terms, int math) {
   return maximum + XLOG(sum, math);
 }
 
-/* SampleLogWeights (src/inference.cc:128-146). Returns size on failure. */
-static size_t SFX(sample_log_weights)(size_t size, const S *terms,
-                                      S normalizer, S uniform, int math) {
-  S cumulative = (S)0;
-  size_t last_supported = size;
-  for (size_t index = 0; index < size; ++index) {
-    const S log_weight = terms[index];
-    if (!isfinite(log_weight))
-      continue;
-    last_supported = index;
-    cumulative += XEXP(log_weight - normalizer, math);
-    if (uniform < cumulative)
-      return index;
-  }
-  return last_supported;
-}
-
 /* Argmax (src/inference.cc:112-126): first maximum wins. */
 static size_t SFX(argmax)(size_t size, const S *terms, S *maximum) {
   size_t result = 0;
@@ -170,6 +157,49 @@ static size_t SFX(argmax)(size_t size, const S *terms, S *maximum) {
   }
   *maximum = value;
   return result;
+}
+
+/* Gap between the chosen maximum and the best other term, relative to the
+ * magnitude of the maximum (max(1, |maximum|)): the margin of the deciding
+ * comparison of an argmax (+inf when no other term is finite). Diagnostic
+ * only; not part of the reference algorithm. */
+static S SFX(runner_up_gap)(size_t size, const S *terms, size_t chosen) {
+  S second = (S)(-INFINITY);
+  for (size_t index = 0; index < size; ++index)
+    if (index != chosen && terms[index] > second)
+      second = terms[index];
+  if (!isfinite(second))
+    return (S)INFINITY;
+  const S scale = fabs(terms[chosen]) > (S)1 ? fabs(terms[chosen]) : (S)1;
+  return (terms[chosen] - second) / scale;
+}
+
+/* SampleLogWeights (src/inference.cc:128-146). Returns size on failure.
+ * Also reports the margin of its deciding comparisons, the distance from the
+ * uniform to the nearer end of the chosen state's cumulative interval
+ * (diagnostic only; the draw is the reference's). */
+static size_t SFX(sample_log_weights)(size_t size, const S *terms,
+                                      S normalizer, S uniform, int math,
+                                      S *margin) {
+  S cumulative = (S)0;
+  S below = (S)0;
+  size_t last_supported = size;
+  for (size_t index = 0; index < size; ++index) {
+    const S log_weight = terms[index];
+    if (!isfinite(log_weight))
+      continue;
+    last_supported = index;
+    below = cumulative;
+    cumulative += XEXP(log_weight - normalizer, math);
+    if (uniform < cumulative) {
+      const S up = cumulative - uniform;
+      const S down = uniform - below;
+      *margin = below == (S)0 ? up : (up < down ? up : down);
+      return index;
+    }
+  }
+  *margin = uniform - cumulative;
+  return last_supported;
 }
 
 static const uint32_t *SFX(op)(const uint32_t *base, size_t width,
@@ -512,6 +542,8 @@ static void SFX(max_batch)(const oracle_plan *plan, SFX(store) * st,
         for (size_t c = 0; c < K; ++c)
           terms[c] = path[p * K + c] + leaf[c];
         choices[p] = (uint32_t)SFX(argmax)(K, terms, &message[p]);
+        if (st->rake_margins != NULL)
+          st->rake_margins[(size_t)op[2] * K + p] = SFX(runner_up_gap)(K, terms, choices[p]);
       }
     }
     break;
@@ -533,6 +565,9 @@ static void SFX(max_batch)(const oracle_plan *plan, SFX(store) * st,
             terms[m] = st->scratch[p * K + m] + middle[m] + right[m * K + c];
           choices[p * K + c] =
               (uint32_t)SFX(argmax)(K, terms, &left[p * K + c]);
+          if (st->compression_margins != NULL)
+            st->compression_margins[(size_t)op[3] * KK + p * K + c] =
+                SFX(runner_up_gap)(K, terms, choices[p * K + c]);
         }
       }
     }
@@ -630,11 +665,17 @@ int SFX(oracle_marginals)(const oracle_plan *plan, size_t states,
   return status;
 }
 
-int SFX(oracle_map)(const oracle_plan *plan, size_t states, const S *nodes,
-                    const S *edges, int math, S *log_weight,
-                    uint32_t *assignment) {
+int SFX(oracle_map_margins)(const oracle_plan *plan, size_t states, const S *nodes,
+                            const S *edges, int math, S *log_weight,
+                            uint32_t *assignment, S *margins) {
   SFX(store) st;
   int status = SFX(prepare)(plan, states, nodes, edges, 0, 0, 1, &st);
+  if (status == ORACLE_OK && margins != NULL) {
+    st.rake_margins = SFX(zeros)((size_t)plan->num_rakes * states);
+    st.compression_margins = SFX(zeros)((size_t)plan->num_compressions * st.matrix);
+    if (st.rake_margins == NULL || st.compression_margins == NULL)
+      status = ORACLE_NO_MEMORY;
+  }
   if (status == ORACLE_OK) {
     st.math = math;
     SFX(take_logs)(plan, &st);
@@ -645,6 +686,9 @@ int SFX(oracle_map)(const oracle_plan *plan, size_t states, const S *nodes,
     /* FinishRoot, src/inference.cc:641-649 */
     assignment[plan->root] = (uint32_t)SFX(argmax)(
         states, NODE(&st, plan->root), &st.max_log_weight);
+    if (margins != NULL)
+      margins[plan->root] =
+          SFX(runner_up_gap)(states, NODE(&st, plan->root), assignment[plan->root]);
     if (!isfinite(st.max_log_weight))
       status = ORACLE_DOMAIN_ERROR;
   }
@@ -657,14 +701,17 @@ int SFX(oracle_map)(const oracle_plan *plan, size_t states, const S *nodes,
           const uint32_t *op = SFX(op)(plan->rakes, 4, i);
           assignment[op[1]] =
               st.rake_choices[(size_t)op[2] * states + assignment[op[3]]];
+          if (margins != NULL)
+            margins[op[1]] = st.rake_margins[(size_t)op[2] * states + assignment[op[3]]];
         }
       } else if (batch[0] == 3) {
         for (uint32_t i = batch[1]; i < batch[1] + batch[2]; ++i) {
           const uint32_t *op = SFX(op)(plan->compressions, 6, i);
-          assignment[op[1]] =
-              st.compression_choices[(size_t)op[3] * st.matrix +
-                                     (size_t)assignment[op[4]] * states +
-                                     assignment[op[5]]];
+          const size_t entry = (size_t)op[3] * st.matrix +
+                               (size_t)assignment[op[4]] * states + assignment[op[5]];
+          assignment[op[1]] = st.compression_choices[entry];
+          if (margins != NULL)
+            margins[op[1]] = st.compression_margins[entry];
         }
       }
     }
@@ -674,9 +721,16 @@ int SFX(oracle_map)(const oracle_plan *plan, size_t states, const S *nodes,
   return status;
 }
 
-int SFX(oracle_sample)(const oracle_plan *plan, size_t states, const S *nodes,
-                       const S *edges, const S *uniforms, int math,
-                       uint32_t *assignment) {
+int SFX(oracle_map)(const oracle_plan *plan, size_t states, const S *nodes,
+                    const S *edges, int math, S *log_weight,
+                    uint32_t *assignment) {
+  return SFX(oracle_map_margins)(plan, states, nodes, edges, math, log_weight,
+                                 assignment, NULL);
+}
+
+int SFX(oracle_sample_margins)(const oracle_plan *plan, size_t states, const S *nodes,
+                               const S *edges, const S *uniforms, int math,
+                               uint32_t *assignment, S *margins) {
   SFX(store) st;
   int status = SFX(prepare)(plan, states, nodes, edges, 0, 1, 0, &st);
   S terms[256];
@@ -696,9 +750,12 @@ int SFX(oracle_sample)(const oracle_plan *plan, size_t states, const S *nodes,
         status = ORACLE_INVALID_ARGUMENT;
   }
   if (status == ORACLE_OK) {
+    S gap = (S)0;
     size_t choice = SFX(sample_log_weights)(states, NODE(&st, plan->root),
-                                            st.log_partition,
-                                            uniforms[plan->root], math);
+                                                   st.log_partition,
+                                                   uniforms[plan->root], math, &gap);
+    if (margins != NULL)
+      margins[plan->root] = gap;
     if (choice == states)
       status = ORACLE_DOMAIN_ERROR;
     assignment[plan->root] = (uint32_t)choice;
@@ -715,10 +772,12 @@ int SFX(oracle_sample)(const oracle_plan *plan, size_t states, const S *nodes,
             terms[c] = path[p * states + c] + leaf[c];
           const S normalizer = SFX(log_sum_exp)(states, terms, math);
           choice = SFX(sample_log_weights)(states, terms, normalizer,
-                                           uniforms[op[1]], math);
+                                                  uniforms[op[1]], math, &gap);
           if (choice == states)
             status = ORACLE_DOMAIN_ERROR;
           assignment[op[1]] = (uint32_t)choice;
+          if (margins != NULL)
+            margins[op[1]] = gap;
         }
       } else if (batch[0] == 3) {
         for (uint32_t i = batch[1]; i < batch[1] + batch[2]; ++i) {
@@ -732,16 +791,25 @@ int SFX(oracle_sample)(const oracle_plan *plan, size_t states, const S *nodes,
             terms[m] = left[p * states + m] + middle[m] + right[m * states + c];
           const S normalizer = SFX(log_sum_exp)(states, terms, math);
           choice = SFX(sample_log_weights)(states, terms, normalizer,
-                                           uniforms[op[1]], math);
+                                                  uniforms[op[1]], math, &gap);
           if (choice == states)
             status = ORACLE_DOMAIN_ERROR;
           assignment[op[1]] = (uint32_t)choice;
+          if (margins != NULL)
+            margins[op[1]] = gap;
         }
       }
     }
   }
   SFX(store_free)(&st);
   return status;
+}
+
+int SFX(oracle_sample)(const oracle_plan *plan, size_t states, const S *nodes,
+                       const S *edges, const S *uniforms, int math,
+                       uint32_t *assignment) {
+  return SFX(oracle_sample_margins)(plan, states, nodes, edges, uniforms, math,
+                                    assignment, NULL);
 }
 
 #undef NODE

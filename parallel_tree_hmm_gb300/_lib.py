@@ -177,6 +177,7 @@ PROTOTYPES = {
     "thmm_workspace_stream": (c_void_p, [c_void_p]),
     "thmm_workspace_synchronize": (c_int, [c_void_p]),
     "thmm_workspace_launches": (c_u64, [c_void_p]),
+    "thmm_wait_timeout_check": (c_int, [c_int, c_u64]),
     "thmm_log_partition_static": (c_int, [c_void_p, c_size, c_size, c_void_p, c_void_p,
                                           c_void_p, c_void_p]),
 }

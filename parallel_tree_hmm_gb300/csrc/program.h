@@ -94,6 +94,10 @@ THMM_DECLARE_LAUNCHER(LaunchSampleF64)
 // Tensor-core sum-product kernels for 32 < K <= 128 (kmax 64 or 128, FP32).
 cudaError_t LaunchWide(unsigned kmax, int part, const EngineArgs &args, int grid,
                        cudaStream_t stream, int *blocks_per_sm);
+// One warp whose bounded mbarrier wait cannot complete and gives up after
+// `budget` cycles, setting kErrorTensorTimeout in *error.
+cudaError_t LaunchWaitTimeoutCheck(std::uint32_t *error, long long budget,
+                                   cudaStream_t stream);
 
 inline unsigned PaddedStates(std::size_t states) {
   return states <= 4    ? 4u

@@ -1891,6 +1891,25 @@ thmm_status thmm_workspace_synchronize(thmm_workspace *workspace) {
   });
 }
 
+thmm_status thmm_wait_timeout_check(int device, uint64_t cycles) {
+  return Guard([&] {
+    if (cycles == 0 || cycles > (1ull << 34))
+      throw std::invalid_argument("wait budget must be between 1 and 2^34 cycles");
+    thmm::Check(cudaSetDevice(device), "cudaSetDevice");
+    thmm::DeviceBuffer error;
+    error.Allocate(sizeof(std::uint32_t));
+    thmm::Check(cudaMemset(error.ptr, 0, sizeof(std::uint32_t)), "cudaMemset");
+    thmm::Check(thmm::LaunchWaitTimeoutCheck(error.as<std::uint32_t>(),
+                                             static_cast<long long>(cycles), nullptr),
+                "wait check launch");
+    std::uint32_t bits = 0;
+    thmm::Check(cudaMemcpy(&bits, error.ptr, sizeof bits, cudaMemcpyDeviceToHost),
+                "wait check result");
+    if (bits & thmm::kErrorTensorTimeout)
+      throw std::runtime_error("tree-HMM accelerator tensor-core wait timed out");
+  });
+}
+
 uint64_t thmm_workspace_launches(const thmm_workspace *workspace) {
   return workspace == nullptr
              ? 0

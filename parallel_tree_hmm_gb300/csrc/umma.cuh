@@ -101,9 +101,13 @@ __device__ __forceinline__ void Commit(std::uint64_t *barrier) {
       : "memory");
 }
 
-// Waits for phase `parity` of `barrier` to complete, for at most about 2^31
-// SM cycles (about a second). Returns false on time-out.
-__device__ __forceinline__ bool Wait(std::uint64_t *barrier, std::uint32_t parity) {
+// Default wait budget: about 2^31 SM cycles (about a second at 2 GHz).
+inline constexpr long long kWaitCycles = 1ll << 31;
+
+// Waits for phase `parity` of `barrier` to complete, for at most `budget` SM
+// cycles. Returns false on time-out.
+__device__ __forceinline__ bool Wait(std::uint64_t *barrier, std::uint32_t parity,
+                                     long long budget = kWaitCycles) {
   const long long start = clock64();
   std::uint32_t done = 0;
   while (true) {
@@ -114,7 +118,7 @@ __device__ __forceinline__ bool Wait(std::uint64_t *barrier, std::uint32_t parit
                  : "memory");
     if (done)
       return true;
-    if (clock64() - start > (1ll << 31))
+    if (clock64() - start > budget)
       return false;
   }
 }

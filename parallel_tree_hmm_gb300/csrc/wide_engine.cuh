@@ -207,7 +207,15 @@ template <int KP> __device__ __forceinline__ void ClearOperands(unsigned char *s
 //   D[r][n] = sum_{d < K} X(r, d) * Y(n, d)
 // for r, n < K (other lanes and columns hold values nobody reads), in 3xTF32
 // with FP32 accumulation. Returns false if a tensor-core wait timed out.
-template <int KP, class XS, class YS>
+//
+// With kSplit, the product is left in KP / kChunk + 1 accumulators of KP
+// columns each instead of one: the hi*hi part of depth chunk c at column
+// c * KP, and both small parts (lo*hi + hi*lo) of every chunk at column
+// (KP / kChunk) * KP; SplitSum32 adds them in FP32. Each accumulator then
+// takes at most 16 tensor-core steps instead of 48 at K = 128, and the
+// tensor core's accumulation error grows with the steps accumulated into one
+// accumulator (about 1.7e-6 relative on log Z at K = 128 with one).
+template <int KP, class XS, class YS, bool kSplit = false>
 __device__ bool Product(unsigned char *smem, Shared &sh, std::uint32_t &phase,
                         std::uint32_t tmem, unsigned K, const XS &x, const YS &y) {
   static_assert(KP % kChunk == 0 && KP <= 128, "padded state count");
@@ -237,7 +245,14 @@ __device__ bool Product(unsigned char *smem, Shared &sh, std::uint32_t &phase,
         for (unsigned k = 0; k < kChunk / 8; ++k) {
           const std::uint64_t a = umma::SmemDescriptor(a_parts[part] + k * 256, kSbo);
           const std::uint64_t b = umma::SmemDescriptor(b_parts[part] + k * 256, kSbo);
-          umma::MmaTf32(tmem, a, b, kDescriptor, chunk != 0 || part != 0 || k != 0);
+          if constexpr (kSplit) {
+            const bool big = part == 2;
+            const std::uint32_t column = big ? chunk * KP : (KP / kChunk) * KP;
+            const bool accumulate = big ? k != 0 : (chunk != 0 || part != 0 || k != 0);
+            umma::MmaTf32(tmem + column, a, b, kDescriptor, accumulate);
+          } else {
+            umma::MmaTf32(tmem, a, b, kDescriptor, chunk != 0 || part != 0 || k != 0);
+          }
         }
       }
       umma::Commit(&sh.barrier);
@@ -247,6 +262,23 @@ __device__ bool Product(unsigned char *smem, Shared &sh, std::uint32_t &phase,
     umma::FenceAfterSync();
   }
   return ok;
+}
+
+// Columns [c, c + 32) of this thread's lane of a split product (Product with
+// kSplit at `lane_base`): the hi*hi accumulators of the depth chunks in order,
+// then the small-part accumulator, added in FP32.
+template <int KP>
+__device__ __forceinline__ void SplitSum32(std::uint32_t lane_base, unsigned c,
+                                           float (&row)[32]) {
+  umma::Load32(lane_base + c, row);
+#pragma unroll 1
+  for (unsigned part = 1; part <= KP / kChunk; ++part) {
+    float more[32];
+    umma::Load32(lane_base + part * KP + c, more);
+#pragma unroll
+    for (unsigned q = 0; q < 32; ++q)
+      row[q] += more[q];
+  }
 }
 
 } // namespace wide

@@ -74,8 +74,12 @@ template <int KP> __device__ void Tree<KP>::Forward() {
         }
         __syncthreads();
         // X(r, d) = left[r][d] * middle[d]; Y(n, d) = right[d][n].
-        ok = Product<KP>(smem, sh, phase, tmem + Layout<KP>::kProductColumn, K,
-                         RowMajor{left, middle}, Transposed{right}) &&
+        // Split accumulators (see Product): log Z is formed from these
+        // products alone, so they get the more accurate accumulation.
+        ok = Product<KP, RowMajor, Transposed, true>(smem, sh, phase,
+                                                     tmem + Layout<KP>::kProductColumn, K,
+                                                     RowMajor{left, middle},
+                                                     Transposed{right}) &&
              ok;
         // Row j of the product is tensor-memory lane j: maximum, then scale.
         const std::uint32_t lane_base =
@@ -84,7 +88,7 @@ template <int KP> __device__ void Tree<KP>::Forward() {
 #pragma unroll 1
         for (unsigned c = 0; c < KP; c += 32) {
           float row[32];
-          umma::Load32(lane_base + c, row);
+          SplitSum32<KP>(lane_base, c, row);
 #pragma unroll
           for (unsigned q = 0; q < 32; ++q)
             if (j < K && c + q < K)
@@ -95,7 +99,7 @@ template <int KP> __device__ void Tree<KP>::Forward() {
 #pragma unroll 1
         for (unsigned c = 0; c < KP; c += 32) {
           float row[32];
-          umma::Load32(lane_base + c, row);
+          SplitSum32<KP>(lane_base, c, row);
 #pragma unroll
           for (unsigned q = 0; q < 32; ++q)
             if (j < K && c + q < K)
