@@ -515,10 +515,16 @@ class GaltonWatsonForest:
     with a Dirichlet(2) emission table, Dirichlet(0.3) edge rows, Dirichlet(1)
     root factor and one U[0,1) variate per node."""
 
-    def __init__(self, trees: int, states: int, seed: int):
+    # Above this many edge rows the Dirichlet rows are drawn on the GPU
+    # (torch) straight into the caller's buffer instead of by numpy on the
+    # host: 16,384 trees hold about 27 G gamma variates.
+    DEVICE_ROWS = 1 << 28
+
+    def __init__(self, trees: int, states: int, seed: int, edges_on_device: bool = False):
         from parallel_tree_hmm_gb300 import synthetic
 
         rng = np.random.default_rng(seed)
+        self.seed = seed
         self.parents = [synthetic.galton_watson(rng) for _ in range(trees)]
         self.states = states
         self.observed = [synthetic.leaves(p) for p in self.parents]
@@ -529,12 +535,38 @@ class GaltonWatsonForest:
         K = states
         self.root = synthetic.dirichlet_rows(rng, 1, K, 1.0, np.float32).ravel()
         self.emission = synthetic.dirichlet_rows(rng, K, K, 2.0, np.float32).ravel()
-        g = rng.standard_gamma(0.3, size=(self.total_edges * K, K), dtype=np.float32)
-        g /= g.sum(axis=1, keepdims=True)
-        np.nan_to_num(g, copy=False, nan=1.0 / K)
-        self.edges = g.ravel()
+        self.edges_on_device = edges_on_device and self.total_edges * K > self.DEVICE_ROWS
+        if self.edges_on_device:
+            self.edges = None  # fill_edges() writes them into the caller's buffer
+        else:
+            g = rng.standard_gamma(0.3, size=(self.total_edges * K, K), dtype=np.float32)
+            g /= g.sum(axis=1, keepdims=True)
+            np.nan_to_num(g, copy=False, nan=1.0 / K)
+            self.edges = g.ravel()
         self.observations = rng.integers(0, K, size=self.total_observed, dtype=np.uint8)
         self.uniforms = rng.random(self.total_nodes, dtype=np.float32)
+
+    def fill_edges(self, out: np.ndarray, device: int) -> None:
+        """Dirichlet(0.3) edge rows drawn on the GPU in chunks and copied into
+        `out` (float32, every edge's K x K matrix); afterwards self.edges is
+        `out`."""
+        import torch
+
+        K = self.states
+        rows = self.total_edges * K
+        generator = torch.Generator(device=f"cuda:{device}")
+        generator.manual_seed(self.seed)
+        target = torch.from_numpy(out)
+        chunk = 1 << 24
+        alpha = torch.full((chunk, K), 0.3, dtype=torch.float32, device=f"cuda:{device}")
+        for start in range(0, rows, chunk):
+            n = min(chunk, rows - start)
+            g = torch._standard_gamma(alpha[:n], generator=generator)
+            g /= g.sum(dim=1, keepdim=True)
+            torch.nan_to_num_(g, nan=1.0 / K)
+            target[start * K:(start + n) * K].copy_(g.reshape(-1))
+        torch.cuda.synchronize(device)
+        self.edges = out
 
     def tree_inputs(self, t, dtype):
         """Dense node factors, edge factors and uniforms of tree t."""
@@ -554,7 +586,17 @@ class GaltonWatsonForest:
             dense32[self.observed[t]] = (dense32[self.observed[t]] *
                                          self.emission.reshape(K, K)[obs])
             dense = dense32
-        edges = self.edges[edge0 * K * K:(edge0 + n - 1) * K * K].astype(dtype)
+        if self.edges is None:
+            # Edges drawn on the device were never made on this host (the CPU
+            # reference arm of a large forest): the tree's own Dirichlet(0.3)
+            # rows from a per-tree seed, same law.
+            rng = np.random.default_rng([self.seed, t])
+            g = rng.standard_gamma(0.3, size=((n - 1) * K, K))
+            g /= g.sum(axis=1, keepdims=True)
+            np.nan_to_num(g, copy=False, nan=1.0 / K)
+            edges = g.ravel().astype(dtype)
+        else:
+            edges = self.edges[edge0 * K * K:(edge0 + n - 1) * K * K].astype(dtype)
         return dense.ravel().astype(dtype), edges, self.uniforms[node0:node0 + n]
 
 
@@ -562,7 +604,8 @@ def run_gw(args, rank, world, local_rank, dist):
     import parallel_tree_hmm_gb300 as thmm
     from oracle import bridge
 
-    forest = GaltonWatsonForest(args.trees, args.states, rank_seed(args.seed, rank))
+    forest = GaltonWatsonForest(args.trees, args.states, rank_seed(args.seed, rank),
+                                edges_on_device=True)
     K = forest.states
     config = {
         "workload": (f"Galton-Watson forest: {args.trees} Poisson(2) trees of "
@@ -617,7 +660,10 @@ def run_gw(args, rank, world, local_rank, dist):
     staged = ws.categorical_inputs()
     staged.root_potential[:] = forest.root
     staged.emission_potentials[:] = forest.emission
-    staged.edge_potentials[:] = forest.edges
+    if forest.edges_on_device:
+        forest.fill_edges(staged.edge_potentials, device)
+    else:
+        staged.edge_potentials[:] = forest.edges
     staged.observations[:] = forest.observations
     uniforms = ws.uniforms()
     uniforms[:] = forest.uniforms

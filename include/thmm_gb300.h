@@ -341,8 +341,12 @@ thmm_status thmm_enqueue(thmm_workspace *workspace, int operation,
  * THMM_SCHEDULE_TEAMS contracts each tree with one CTA or warp walking its
  * plan step by step; THMM_SCHEDULE_PHASES runs each round of every tree in
  * one grid-wide launch per operation kind (the default where available).
- * Other workspaces always use THMM_SCHEDULE_TEAMS. No setting changes any
- * result bit. */
+ * Other workspaces always use THMM_SCHEDULE_TEAMS. Under
+ * THMM_SCHEDULE_PHASES, the first `phase_rounds` rounds run as grid-wide
+ * launches and the remaining rounds of each tree of a forest run in one warp
+ * per tree (0: chosen from the operation counts; at least the tree's round
+ * count: every round grid-wide; the batch API's shared-topology layout runs
+ * every round grid-wide). No setting changes any result bit. */
 #define THMM_SCHEDULE_TEAMS 0
 #define THMM_SCHEDULE_PHASES 1
 typedef struct thmm_tuning {
@@ -352,6 +356,7 @@ typedef struct thmm_tuning {
   float kernel_ms;     /* device time per step of the chosen setting */
   uint32_t candidates; /* settings timed by the last autotune */
   uint32_t schedule;   /* THMM_SCHEDULE_TEAMS or THMM_SCHEDULE_PHASES */
+  uint32_t phase_rounds; /* grid-wide rounds of THMM_SCHEDULE_PHASES; 0: automatic */
 } thmm_tuning;
 /* Times candidate settings for `operation` on the inputs left resident by a
  * prepared call (`repeats` timed steps each, after one untimed step), keeps

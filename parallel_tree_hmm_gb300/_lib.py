@@ -115,7 +115,7 @@ class MarginalResult(ctypes.Structure):
 class Tuning(ctypes.Structure):
     _fields_ = [("team_threshold", c_u32), ("ctas_per_sm", c_u32 * 4),
                 ("stripes", c_u32), ("kernel_ms", ctypes.c_float), ("candidates", c_u32),
-                ("schedule", c_u32)]
+                ("schedule", c_u32), ("phase_rounds", c_u32)]
 
 
 # name -> (restype, argtypes)

@@ -512,17 +512,24 @@ class Workspace:
         return _tuning_dict(tuning)
 
     def set_tuning(self, team_threshold: int, ctas_per_sm=(0, 0, 0, 0),
-                   stripes: int = 0, schedule: int | None = None) -> None:
+                   stripes: int = 0, schedule: int | None = None,
+                   phase_rounds: int | None = None) -> None:
         """Applies a launch tuning. `schedule` (THMM_SCHEDULE_TEAMS or
-        THMM_SCHEDULE_PHASES) defaults to the workspace's current one."""
+        THMM_SCHEDULE_PHASES) and `phase_rounds` (grid-wide rounds of the
+        phase schedule, 0 automatic) default to the workspace's current
+        ones."""
+        current = self.tuning
         if schedule is None:
-            schedule = self.tuning["schedule"]
+            schedule = current["schedule"]
+        if phase_rounds is None:
+            phase_rounds = current["phase_rounds"]
         tuning = _lib.Tuning()
         tuning.team_threshold = team_threshold
         for i, value in enumerate(ctas_per_sm):
             tuning.ctas_per_sm[i] = value
         tuning.stripes = stripes
         tuning.schedule = schedule
+        tuning.phase_rounds = phase_rounds
         _check(self._lib.thmm_set_tuning(self._handle, ctypes.byref(tuning)))
 
     @property
@@ -542,7 +549,7 @@ def _tuning_dict(tuning) -> dict:
             "ctas_per_sm": [int(v) for v in tuning.ctas_per_sm],
             "stripes": int(tuning.stripes),
             "kernel_ms": float(tuning.kernel_ms), "candidates": int(tuning.candidates),
-            "schedule": int(tuning.schedule)}
+            "schedule": int(tuning.schedule), "phase_rounds": int(tuning.phase_rounds)}
 
 
 def available() -> bool:

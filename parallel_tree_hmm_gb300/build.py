@@ -141,6 +141,10 @@ def build_oracle(reference: bool = True) -> None:
     ref = os.environ.get("THMM_REFERENCE", str(ROOT.parent / "reference"))
     if reference and os.path.isdir(os.path.join(ref, "src")):
         subprocess.run(["make", "-s", "-C", str(oracle_dir), "ref", f"REF={ref}"], check=True)
+        # Copies of the reference's accelerator suite for machines without
+        # the reference tree (built there by tests/test_gpu_ref_suite.py).
+        subprocess.run(["make", "-s", "-C", str(oracle_dir), "ref-suite-stage", f"REF={ref}"],
+                       check=True)
 
 
 if __name__ == "__main__":

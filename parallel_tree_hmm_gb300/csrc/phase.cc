@@ -72,6 +72,46 @@ PhasePlan::OpRange(int kind, std::uint32_t round, std::uint32_t a, std::uint32_t
   return {first, last};
 }
 
+PhasePlan::Tail PhasePlan::BuildTail(std::uint32_t tail_round) const {
+  Tail tail;
+  const std::size_t n = instance_program.size();
+  std::vector<std::uint64_t> gather_at(rounds, 0), rake_at(rounds, 0),
+      compress_at(rounds, 0);
+  for (std::uint32_t r = 0; r < rounds; ++r) {
+    gather_at[r] = gather_base[r];
+    rake_at[r] = rake_base[r];
+    compress_at[r] = compress_base[r];
+  }
+  for (std::size_t i = 0; i < n; ++i) {
+    const ProgramRounds &c = program_rounds[instance_program[i]];
+    if (c.rounds > tail_round) {
+      tail.items.push_back({static_cast<std::uint32_t>(i),
+                            static_cast<std::uint32_t>(tail.rounds.size()),
+                            c.rounds - tail_round, 0u});
+      for (std::uint32_t r = tail_round; r < c.rounds; ++r) {
+        tail.rounds.push_back({static_cast<std::uint32_t>(gather_at[r]), c.gathers[r],
+                               static_cast<std::uint32_t>(compress_at[r]),
+                               c.compressions[r]});
+        tail.rakes.push_back({static_cast<std::uint32_t>(rake_at[r]), c.rakes[r]});
+      }
+    }
+    for (std::uint32_t r = 0; r < c.rounds; ++r) {
+      gather_at[r] += c.gathers[r];
+      rake_at[r] += c.rakes[r];
+      compress_at[r] += c.compressions[r];
+    }
+  }
+  return tail;
+}
+
+std::uint32_t PhasePlan::AutoTailRound(std::uint64_t ops) const {
+  for (std::uint32_t r = 0; r < rounds; ++r)
+    if ((gather_base[r + 1] - gather_base[r]) + (compress_base[r + 1] - compress_base[r]) <
+        ops)
+      return r;
+  return rounds;
+}
+
 PhasePlan BuildPhasePlan(const ProgramSet &set, std::span<const PhaseInstance> instances,
                          std::uint64_t total_nodes, std::uint64_t total_edges_out,
                          unsigned threads) {
@@ -207,6 +247,40 @@ PhasePlan BuildPhasePlan(const ProgramSet &set, std::span<const PhaseInstance> i
       if (error)
         std::rethrow_exception(error);
   }
+
+  // Observation reads in the order the phases make them. Each observed node's
+  // input factor is read by exactly one record: the first-absorption gather
+  // of the node, the rake of a leaf with nothing absorbed, the compression of
+  // a middle node with nothing absorbed, or the root record. Those records
+  // get consecutive slots of a phase-ordered copy of the observations (the
+  // runtime gathers it from the caller's array whenever observations are
+  // uploaded), so the phases read their observation bytes sequentially
+  // instead of one scattered byte per 32-byte sector; every other record's
+  // observation field becomes kNone.
+  const auto take = [&](std::uint32_t &field, bool reads) {
+    if (reads && field != kNone) {
+      plan.observation_order.push_back(field);
+      field = static_cast<std::uint32_t>(plan.observation_order.size() - 1);
+    } else {
+      field = kNone;
+    }
+  };
+  for (std::uint32_t r = 0; r < rounds; ++r) {
+    for (std::uint64_t g = plan.gather_base[r]; g < plan.gather_base[r + 1]; ++g) {
+      Uint4 &gather = plan.gathers[g];
+      take(gather.y, (gather.x & kFlag) != 0);
+      for (std::uint32_t k = 0; k < (gather.w & kCountMask); ++k) {
+        Uint4 &rake = plan.rakes[gather.z + k];
+        take(rake.z, (rake.y & kFlag) == 0);
+      }
+    }
+    for (std::uint64_t c = plan.compress_base[r]; c < plan.compress_base[r + 1]; ++c)
+      take(plan.compress[c].w, (plan.compress[c].y & kFlag) == 0);
+  }
+  for (Uint2 &root : plan.roots)
+    take(root.y, (root.x & kFlag) == 0);
+  if (plan.observation_order.size() >= kIndexLimit)
+    return PhasePlan{};
 
   plan.rounds = rounds;
   plan.total_compressions = plan.compress_base[rounds];

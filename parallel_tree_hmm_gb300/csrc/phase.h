@@ -44,7 +44,19 @@ enum PhaseKind : int {
   kPhaseFinish = 2,          // log Z (and the root marginal) per instance
   kPhaseRakeReverse = 3,     // adjoint of the round's rakes
   kPhaseCompressReverse = 4, // adjoint of the round's compressions
+  kPhaseTailForward = 5,     // rounds >= the tail round, one warp per tree
+  kPhaseTailReverse = 6,     // their adjoint, one warp per tree
 };
+
+// The last rounds of a forest hold few operations (rounds 5 and later of the
+// uneven K=4 forest hold 0.4 % of them) but one launch each, and a launch
+// costs microseconds however little it does. From the tail round on, the
+// schedule can switch to one warp per tree that walks the tree's remaining
+// rounds with a warp barrier between steps (the same operation functions,
+// so the same bits). Tail records:
+//   tail item   uint4: instance, first tail round entry, tail rounds, 0
+//   tail round  uint4: first gather, gathers, first compression, compressions
+//   tail rakes  uint2: first rake, rakes (of the same round)
 
 // Records (absolute indices; kFlag marks a stored value / a compressed path):
 //  rake     uint4: path (edge-out index, or kFlag | global compression),
@@ -54,6 +66,8 @@ enum PhaseKind : int {
 //  compress uint4: left path, middle node (kFlag: stored), right path,
 //                  middle observation; compression i writes path i
 //  root     uint2: root node (kFlag: stored), root observation
+// Observation fields index the phase-ordered copy of the observations
+// (PhasePlan::observation_order), not the caller's array.
 inline constexpr std::uint32_t kRootBit = 0x40000000u;
 inline constexpr std::uint32_t kCountMask = 0x3fffffffu;
 
@@ -83,6 +97,18 @@ struct PhaseArgs {
   void *edge_out;     // edge marginals
   std::uint32_t raw;     // output exp(log Z)
   std::uint32_t reverse; // finish: also write the root marginal
+  const uint4 *tail_items;
+  const uint4 *tail_rounds;
+  const uint2 *tail_rakes;
+  // Shared-topology layout only (BatchPhaseKernel): items [first_item,
+  // first_item + items) of a batch whose stored objects are `item_stride`
+  // items apart, each with item_nodes nodes and item_edges edges.
+  std::uint32_t batch;
+  std::uint32_t first_item;
+  std::uint32_t items;
+  std::uint64_t item_stride;
+  std::uint64_t item_nodes;
+  std::uint64_t item_edges;
 };
 
 // Operation counts of one program per round and kind.
@@ -107,11 +133,24 @@ struct PhasePlan {
   std::vector<ProgramRounds> program_rounds;
   std::vector<std::uint32_t> instance_program;
   std::uint64_t total_compressions = 0;
+  // Caller observation index of each slot of the phase-ordered copy.
+  std::vector<std::uint32_t> observation_order;
 
   // [first, last) operations of round `round` and kind (gather, rake or
   // compress) that belong to instances [a, b).
   std::pair<std::uint64_t, std::uint64_t> OpRange(int kind, std::uint32_t round,
                                                   std::uint32_t a, std::uint32_t b) const;
+
+  // Tail records (see kPhaseTailForward) for rounds >= `tail_round`, over
+  // the instances with more rounds than that, in instance order.
+  struct Tail {
+    std::vector<Uint4> items, rounds;
+    std::vector<Uint2> rakes;
+  };
+  Tail BuildTail(std::uint32_t tail_round) const;
+  // Default tail round: the first round with fewer than `ops` gathers and
+  // compressions over all instances.
+  std::uint32_t AutoTailRound(std::uint64_t ops) const;
 };
 
 struct PhaseInstance {
@@ -132,6 +171,14 @@ PhasePlan BuildPhasePlan(const ProgramSet &set, std::span<const PhaseInstance> i
 // arithmetic. Only padded state count 4 (K <= 4) has a phase schedule.
 cudaError_t LaunchPhase(int scalar_bytes, bool compute_f64, int kind, const PhaseArgs &args,
                         cudaStream_t stream, int *blocks_per_sm);
+
+// The phase-ordered copy of the observations: ordered[j * items + b] =
+// observations[b * per_item + order[j]] for j < count, b < items (a forest:
+// items = 1, per_item = 0).
+cudaError_t LaunchObservationGather(const std::uint8_t *observations,
+                                    const std::uint32_t *order, std::uint8_t *ordered,
+                                    std::uint64_t count, std::uint64_t items,
+                                    std::uint64_t per_item, cudaStream_t stream);
 
 } // namespace thmm
 

@@ -1,6 +1,7 @@
 // Phase kernels of the level-synchronous schedule (phase.h) for padded state
-// count 4 (K <= 4): one thread per operation, the K-vectors and K x K
-// matrices in registers, 16-byte vector loads and stores.
+// count 4 (K <= 4): one thread per operation (one warp per tree in the tail
+// rounds), the K-vectors and K x K matrices in registers, 16-byte vector
+// loads and stores.
 //
 // Each kernel performs exactly the floating-point operations of the
 // one-thread-per-operation (G = 1) branch of LinearEngine (engine.cuh) in
@@ -20,14 +21,62 @@ namespace thmm {
 
 constexpr int kPhaseThreads = 256;
 
-template <typename Scalar, typename Compute> struct PhaseOps {
+// Where the operands of one operation live. Forest layout: the records hold
+// absolute indices of every tree's nodes, edges and compressions, so every
+// map is the identity (a shared edge input is read modulo its edge count).
+struct ForestIndex {
+  __device__ __forceinline__ std::size_t Store(std::uint32_t node) const { return node; }
+  __device__ __forceinline__ std::size_t Io(std::uint32_t node) const { return node; }
+  __device__ __forceinline__ std::size_t Comp(std::uint32_t tape) const { return tape; }
+  __device__ __forceinline__ std::size_t Out(std::uint32_t edge) const { return edge; }
+  __device__ __forceinline__ std::size_t In(const PhaseArgs &a, std::uint32_t edge) const {
+    return a.edge_modulus != 0 ? edge % a.edge_modulus : edge;
+  }
+  __device__ __forceinline__ std::size_t Obs(std::uint32_t slot) const { return slot; }
+};
+
+// Shared-topology layout (the reference's batch API: one plan, B node-factor
+// sets, one edge input): the records are those of ONE tree and are read by
+// every batch item, and consecutive threads take consecutive batch items of
+// the same operation, so a warp reads each record and each edge row once
+// (the addresses coincide) instead of once per item. Stored values are
+// item-minor ([node][item]) so the warp's accesses are contiguous; the
+// phase-ordered observations likewise ([slot][item]). Caller-visible arrays
+// keep the reference's item-major layouts.
+struct BatchIndex {
+  std::uint32_t item;   // batch item of this thread
+  std::uint64_t stride; // items per stored object (the batch capacity)
+  std::uint64_t nodes;  // nodes per item
+  std::uint64_t edges;  // edges per item
+  __device__ __forceinline__ std::size_t Store(std::uint32_t node) const {
+    return node * stride + item;
+  }
+  __device__ __forceinline__ std::size_t Io(std::uint32_t node) const {
+    return item * nodes + node;
+  }
+  __device__ __forceinline__ std::size_t Comp(std::uint32_t tape) const {
+    return tape * stride + item;
+  }
+  __device__ __forceinline__ std::size_t Out(std::uint32_t edge) const {
+    return item * edges + edge;
+  }
+  __device__ __forceinline__ std::size_t In(const PhaseArgs &, std::uint32_t edge) const {
+    return edge;
+  }
+  __device__ __forceinline__ std::size_t Obs(std::uint32_t slot) const {
+    return slot * stride + item;
+  }
+};
+
+template <typename Scalar, typename Compute, class Index> struct PhaseOps {
   static constexpr int KMAX = 4;
   const PhaseArgs &a;
+  Index ix;
   unsigned K;
   unsigned KK;
 
-  __device__ explicit PhaseOps(const PhaseArgs &args)
-      : a(args), K(args.states), KK(args.states * args.states) {}
+  __device__ PhaseOps(const PhaseArgs &args, const Index &index)
+      : a(args), ix(index), K(args.states), KK(args.states * args.states) {}
 
   // Input factor vector of `node`: dense row, or the reference's categorical
   // (root ? root_potential : 1) * emission[observation]
@@ -36,9 +85,7 @@ template <typename Scalar, typename Compute> struct PhaseOps {
                                         Compute (&out)[KMAX]) const {
     Scalar raw[KMAX];
     if (!a.categorical) {
-      LoadRow<KMAX>(static_cast<const Scalar *>(a.node_in) +
-                        static_cast<std::size_t>(node) * K,
-                    K, raw);
+      LoadRow<KMAX>(static_cast<const Scalar *>(a.node_in) + ix.Io(node) * K, K, raw);
     } else {
       const Scalar *root_potential = static_cast<const Scalar *>(a.root_potential);
       if (obs == kNone) {
@@ -46,7 +93,7 @@ template <typename Scalar, typename Compute> struct PhaseOps {
         for (unsigned j = 0; j < KMAX; ++j)
           raw[j] = j < K ? (root ? root_potential[j] : Scalar(1)) : Scalar(0);
       } else {
-        const unsigned category = a.observations[obs];
+        const unsigned category = a.observations[ix.Obs(obs)];
         if (category >= a.categories) {
 #pragma unroll
           for (unsigned j = 0; j < KMAX; ++j)
@@ -71,18 +118,16 @@ template <typename Scalar, typename Compute> struct PhaseOps {
   __device__ __forceinline__ void Node(std::uint32_t ref, std::uint32_t obs,
                                        Compute (&out)[KMAX], int &e) const {
     if (ref & kFlag) {
-      const std::uint32_t node = ref & kMask;
-      LoadRow<KMAX>(static_cast<const Compute *>(a.nodes) + static_cast<std::size_t>(node) * K,
-                    K, out);
-      e += a.node_exp[node];
+      const std::size_t at = ix.Store(ref & kMask);
+      LoadRow<KMAX>(static_cast<const Compute *>(a.nodes) + at * K, K, out);
+      e += a.node_exp[at];
     } else {
       Input(ref, obs, false, out);
     }
   }
 
   __device__ __forceinline__ const Scalar *EdgeIn(std::uint32_t path) const {
-    const std::uint32_t row = a.edge_modulus != 0 ? path % a.edge_modulus : path;
-    return static_cast<const Scalar *>(a.edge_in) + static_cast<std::size_t>(row) * KK;
+    return static_cast<const Scalar *>(a.edge_in) + ix.In(a, path) * KK;
   }
 
   // Row r of path `ref` (zero for padded rows).
@@ -93,15 +138,14 @@ template <typename Scalar, typename Compute> struct PhaseOps {
       for (unsigned j = 0; j < KMAX; ++j)
         out[j] = Compute(0);
     } else if (ref & kFlag) {
-      LoadRow<KMAX>(static_cast<const Compute *>(a.comps) +
-                        static_cast<std::size_t>(ref & kMask) * KK + r * K,
+      LoadRow<KMAX>(static_cast<const Compute *>(a.comps) + ix.Comp(ref & kMask) * KK + r * K,
                     K, out);
     } else {
       LoadRow<KMAX>(EdgeIn(ref) + r * K, K, out);
     }
   }
   __device__ __forceinline__ int PathExp(std::uint32_t ref) const {
-    return (ref & kFlag) ? a.comp_exp[ref & kMask] : 0;
+    return (ref & kFlag) ? a.comp_exp[ix.Comp(ref & kMask)] : 0;
   }
 
   __device__ __forceinline__ static int Exponent(Compute m) {
@@ -112,14 +156,15 @@ template <typename Scalar, typename Compute> struct PhaseOps {
   __device__ __forceinline__ void Gather(std::uint32_t i) const {
     const uint4 op = a.gathers[i];
     const std::uint32_t node = op.x & kMask;
-    Compute *dst = static_cast<Compute *>(a.nodes) + static_cast<std::size_t>(node) * K;
+    const std::size_t at = ix.Store(node);
+    Compute *dst = static_cast<Compute *>(a.nodes) + at * K;
     Compute v[KMAX];
     int e = 0;
     if (op.x & kFlag) {
       Input(node, op.y, (op.w & kRootBit) != 0, v);
     } else {
       LoadRow<KMAX>(dst, K, v);
-      e = a.node_exp[node];
+      e = a.node_exp[at];
     }
     const std::uint32_t count = op.w & kCountMask;
     for (std::uint32_t k = 0; k < count; ++k) {
@@ -155,7 +200,7 @@ template <typename Scalar, typename Compute> struct PhaseOps {
         v[q] = ScalePow2(v[q], -s);
     }
     StoreRow<KMAX>(dst, K, v);
-    a.node_exp[node] = e;
+    a.node_exp[at] = e;
   }
 
   __device__ __forceinline__ void Compress(std::uint32_t i) const {
@@ -193,7 +238,8 @@ template <typename Scalar, typename Compute> struct PhaseOps {
       for (unsigned j = 0; j < KMAX; ++j)
         m = m < out[q][j] ? out[q][j] : m;
     const int s = Exponent(m);
-    Compute *dst = static_cast<Compute *>(a.comps) + static_cast<std::size_t>(i) * KK;
+    const std::size_t at = ix.Comp(i);
+    Compute *dst = static_cast<Compute *>(a.comps) + at * KK;
 #pragma unroll
     for (int q = 0; q < KMAX; ++q) {
       if (q < static_cast<int>(K)) {
@@ -203,19 +249,20 @@ template <typename Scalar, typename Compute> struct PhaseOps {
         StoreRow<KMAX>(dst + q * K, K, out[q]);
       }
     }
-    a.comp_exp[i] = e + s;
+    a.comp_exp[at] = e + s;
   }
 
   // log Z = ln 2 * (root exponent) + log(sum(root)), as LinearEngine::Run.
-  __device__ __forceinline__ void Finish(std::uint32_t i) const {
+  // Root record `i`; the result is instance `value`'s.
+  __device__ __forceinline__ void Finish(std::uint32_t i, std::uint32_t value) const {
     const uint2 rec = a.roots[i];
     const std::uint32_t node = rec.x & kMask;
     Compute root[KMAX];
     long long total = 0;
     if (rec.x & kFlag) {
-      LoadRow<KMAX>(static_cast<const Compute *>(a.nodes) + static_cast<std::size_t>(node) * K,
-                    K, root);
-      total = a.node_exp[node];
+      const std::size_t at = ix.Store(node);
+      LoadRow<KMAX>(static_cast<const Compute *>(a.nodes) + at * K, K, root);
+      total = a.node_exp[at];
     } else {
       Input(node, rec.y, true, root);
     }
@@ -225,9 +272,9 @@ template <typename Scalar, typename Compute> struct PhaseOps {
     const double log_z = !(sum > 0.0)
                              ? -INFINITY
                              : static_cast<double>(total) * 0.6931471805599453094 + log(sum);
-    static_cast<Scalar *>(a.values)[i] = static_cast<Scalar>(a.raw ? exp(log_z) : log_z);
+    static_cast<Scalar *>(a.values)[value] = static_cast<Scalar>(a.raw ? exp(log_z) : log_z);
     if (a.reverse) {
-      Scalar *root_out = static_cast<Scalar *>(a.node_out) + static_cast<std::size_t>(node) * K;
+      Scalar *root_out = static_cast<Scalar *>(a.node_out) + ix.Io(node) * K;
       const bool finite = log_z > -INFINITY;
       for (unsigned j = 0; j < K; ++j) {
         double value = 0.0;
@@ -244,13 +291,11 @@ template <typename Scalar, typename Compute> struct PhaseOps {
   __device__ __forceinline__ void StorePathAdjoint(std::uint32_t ref, unsigned r,
                                                    const Compute (&row)[KMAX]) const {
     if (ref & kFlag)
-      StoreRow<KMAX>(static_cast<Compute *>(a.comp_mu) +
-                         static_cast<std::size_t>(ref & kMask) * KK + r * K,
-                     K, row);
+      StoreRow<KMAX>(static_cast<Compute *>(a.comp_mu) + ix.Comp(ref & kMask) * KK + r * K, K,
+                     row);
     else
-      StoreRowStreaming<KMAX>(static_cast<Scalar *>(a.edge_out) +
-                                  static_cast<std::size_t>(ref) * KK + r * K,
-                              K, row);
+      StoreRowStreaming<KMAX>(static_cast<Scalar *>(a.edge_out) + ix.Out(ref) * KK + r * K, K,
+                              row);
   }
 
   __device__ __forceinline__ void RakeReverse(std::uint32_t i) const {
@@ -260,7 +305,7 @@ template <typename Scalar, typename Compute> struct PhaseOps {
     int unused = 0;
     Node(op.y, op.z, leaf, unused);
     Compute parent_adjoint[KMAX];
-    LoadRow<KMAX>(node_out + static_cast<std::size_t>(op.w) * K, K, parent_adjoint);
+    LoadRow<KMAX>(node_out + ix.Io(op.w) * K, K, parent_adjoint);
     Compute ratio[KMAX];
     Compute rows[KMAX][KMAX];
 #pragma unroll
@@ -288,13 +333,12 @@ template <typename Scalar, typename Compute> struct PhaseOps {
         column = fma(ratio[p], rows[p][j], column);
       adjoint[j] = leaf[j] * column;
     }
-    StoreRow<KMAX>(node_out + static_cast<std::size_t>(op.y & kMask) * K, K, adjoint);
+    StoreRow<KMAX>(node_out + ix.Io(op.y & kMask) * K, K, adjoint);
   }
 
   __device__ __forceinline__ void CompressReverse(std::uint32_t i) const {
     const uint4 op = a.compress[i];
-    const Compute *output_adjoint =
-        static_cast<const Compute *>(a.comp_mu) + static_cast<std::size_t>(i) * KK;
+    const Compute *output_adjoint = static_cast<const Compute *>(a.comp_mu) + ix.Comp(i) * KK;
     Compute middle[KMAX];
     int unused = 0;
     Node(op.y, op.w, middle, unused);
@@ -374,28 +418,90 @@ template <typename Scalar, typename Compute> struct PhaseOps {
       if (mid < K)
         StorePathAdjoint(op.z, mid, right_adjoint);
     }
-    StoreRow<KMAX>(static_cast<Scalar *>(a.node_out) + static_cast<std::size_t>(op.y & kMask) * K,
-                   K, middle_adjoint);
+    StoreRow<KMAX>(static_cast<Scalar *>(a.node_out) + ix.Io(op.y & kMask) * K, K,
+                   middle_adjoint);
   }
 };
 
-template <typename Scalar, typename Compute, int kKind>
-__global__ void __launch_bounds__(kPhaseThreads) PhaseKernel(PhaseArgs args) {
-  const std::uint32_t t = blockIdx.x * kPhaseThreads + threadIdx.x;
-  if (t >= args.count)
-    return;
-  const std::uint32_t i = args.offset + t;
-  const PhaseOps<Scalar, Compute> ops(args);
+// Tail rounds of one tree per warp (kPhaseTailForward / kPhaseTailReverse):
+// the lanes take the operations of a step in turn, with a warp barrier
+// (which also orders the lanes' global-memory accesses) between steps.
+template <typename Scalar, typename Compute, bool kReverse>
+__device__ __forceinline__ void TailTree(const PhaseOps<Scalar, Compute, ForestIndex> &ops,
+                                         const PhaseArgs &a, std::uint32_t item) {
+  const unsigned lane = threadIdx.x & 31u;
+  const uint4 tree = a.tail_items[item];
+  for (std::uint32_t e = 0; e < tree.z; ++e) {
+    const std::uint32_t at = tree.y + (kReverse ? tree.z - 1 - e : e);
+    const uint4 round = a.tail_rounds[at];
+    if constexpr (!kReverse) {
+      for (std::uint32_t i = lane; i < round.y; i += 32)
+        ops.Gather(round.x + i);
+      __syncwarp();
+      for (std::uint32_t i = lane; i < round.w; i += 32)
+        ops.Compress(round.z + i);
+      __syncwarp();
+    } else {
+      for (std::uint32_t i = lane; i < round.w; i += 32)
+        ops.CompressReverse(round.z + i);
+      __syncwarp();
+      const uint2 rakes = a.tail_rakes[at];
+      for (std::uint32_t i = lane; i < rakes.y; i += 32)
+        ops.RakeReverse(rakes.x + i);
+      __syncwarp();
+    }
+  }
+}
+
+template <typename Scalar, typename Compute, class Index, int kKind>
+__device__ __forceinline__ void RunOp(const PhaseArgs &args, const Index &index,
+                                      std::uint32_t i, std::uint32_t value) {
+  const PhaseOps<Scalar, Compute, Index> ops(args, index);
   if constexpr (kKind == kPhaseGather)
     ops.Gather(i);
   else if constexpr (kKind == kPhaseCompress)
     ops.Compress(i);
   else if constexpr (kKind == kPhaseFinish)
-    ops.Finish(i);
+    ops.Finish(i, value);
   else if constexpr (kKind == kPhaseRakeReverse)
     ops.RakeReverse(i);
-  else
+  else if constexpr (kKind == kPhaseCompressReverse)
     ops.CompressReverse(i);
+}
+
+// Forest layout: thread t runs operation offset + t (finish: instance), or
+// warp w the tail of tree offset + w.
+template <typename Scalar, typename Compute, int kKind>
+__global__ void __launch_bounds__(kPhaseThreads) PhaseKernel(PhaseArgs args) {
+  if constexpr (kKind == kPhaseTailForward || kKind == kPhaseTailReverse) {
+    const std::uint32_t w = blockIdx.x * (kPhaseThreads / 32) + threadIdx.x / 32;
+    if (w >= args.count)
+      return;
+    const PhaseOps<Scalar, Compute, ForestIndex> ops(args, ForestIndex{});
+    TailTree<Scalar, Compute, kKind == kPhaseTailReverse>(ops, args, args.offset + w);
+  } else {
+    const std::uint32_t t = blockIdx.x * kPhaseThreads + threadIdx.x;
+    if (t >= args.count)
+      return;
+    const std::uint32_t i = args.offset + t;
+    RunOp<Scalar, Compute, ForestIndex, kKind>(args, ForestIndex{}, i, i);
+  }
+}
+
+// Shared-topology layout: thread t runs operation offset + t / items of
+// batch item first_item + t % items (finish: the root record for that item).
+template <typename Scalar, typename Compute, int kKind>
+__global__ void __launch_bounds__(kPhaseThreads) BatchPhaseKernel(PhaseArgs args) {
+  const std::uint64_t t = static_cast<std::uint64_t>(blockIdx.x) * kPhaseThreads + threadIdx.x;
+  if (t >= static_cast<std::uint64_t>(args.count) * args.items)
+    return;
+  BatchIndex index;
+  index.item = args.first_item + static_cast<std::uint32_t>(t % args.items);
+  index.stride = args.item_stride;
+  index.nodes = args.item_nodes;
+  index.edges = args.item_edges;
+  const std::uint32_t i = args.offset + static_cast<std::uint32_t>(t / args.items);
+  RunOp<Scalar, Compute, BatchIndex, kKind>(args, index, i, index.item);
 }
 
 } // namespace thmm

@@ -210,6 +210,17 @@ struct Workspace {
   DeviceBuffer phase_rakes, phase_gathers, phase_compress, phase_roots;
   DeviceBuffer node_exp, comp_exp;
   std::uint32_t schedule = THMM_SCHEDULE_TEAMS;
+  // Rounds run as grid-wide phases; later rounds run in one warp per tree
+  // (the tail, phase.h). `tail_instances` lists the tail trees in order.
+  std::uint32_t phase_rounds = 0;
+  DeviceBuffer tail_items, tail_rounds, tail_rakes;
+  std::vector<std::uint32_t> tail_instances;
+  // Phase-ordered copy of the observations (PhasePlan::observation_order),
+  // rebuilt on the device whenever observations are uploaded.
+  DeviceBuffer phase_observations, observation_order;
+  std::uint64_t observation_reads = 0;
+  // The batch API's phase layout: one tree's records for every item.
+  bool phase_batch = false;
   // Operation ranges of each round for an instance range (cached).
   struct PhaseRanges {
     std::uint32_t a, b;
@@ -252,11 +263,16 @@ struct Workspace {
     phase = PhasePlan{};
     phase_ranges.clear();
     schedule = THMM_SCHEDULE_TEAMS;
+    phase_rounds = 0;
+    tail_instances.clear();
+    observation_reads = 0;
+    phase_batch = false;
     for (DeviceBuffer *buffer :
          {&programs, &steps, &rakes, &combines, &absorbs, &compress, &instances,
           &compress_ends, &gathers, &team_order, &stripe_order, &control, &node_in,
           &phase_rakes, &phase_gathers, &phase_compress, &phase_roots, &node_exp,
-          &comp_exp, &edge_in,
+          &comp_exp, &tail_items, &tail_rounds, &tail_rakes, &phase_observations,
+          &observation_order, &edge_in,
           &observations, &root_potential, &emission, &uniforms, &values,
           &node_out, &edge_out, &states_out, &scratch, &bytes})
       buffer->Free();
@@ -451,26 +467,42 @@ struct Workspace {
     gathers.Upload(set.gathers, stream);
     instances.Upload(table, stream);
     team_order.Upload(order, stream);
-    // Phase schedule of the sum-product calls for up to 4 states.
+    // Phase schedule of the sum-product calls for up to 4 states. A forest
+    // gets records for every tree; the batch API (one plan shared by every
+    // item, shared edge input) gets the records of one tree, which every
+    // item reads (the shared-topology layout of phase_engine.cuh).
     if (PaddedStates(states) == 4) {
-      std::vector<PhaseInstance> phase_instances(count);
-      for (std::size_t i = 0; i < count; ++i)
+      phase_batch = shared_edges;
+      std::vector<PhaseInstance> phase_instances(phase_batch ? 1 : count);
+      for (std::size_t i = 0; i < phase_instances.size(); ++i)
         phase_instances[i] = {table[i].program, table[i].node_base, table[i].edge_out_base,
                               table[i].obs_base};
-      phase = BuildPhasePlan(set, phase_instances, total_nodes, total_edges_out, 0);
+      phase = phase_batch
+                  ? BuildPhasePlan(set, phase_instances, nodes_per_item, edges_per_item, 0)
+                  : BuildPhasePlan(set, phase_instances, total_nodes, total_edges_out, 0);
+      // Stored objects of the batch layout are item-minor over the capacity.
+      const std::uint64_t copies = phase_batch ? count : 1;
+      if (phase.enabled && phase_batch &&
+          (total_nodes >= kFlag || phase.total_compressions * copies >= kFlag))
+        phase = PhasePlan{};
       if (phase.enabled) {
         phase_rakes.Upload(phase.rakes, stream);
         phase_gathers.Upload(phase.gathers, stream);
         phase_compress.Upload(phase.compress, stream);
         phase_roots.Upload(phase.roots, stream);
         node_exp.Allocate(total_nodes * sizeof(int));
-        comp_exp.Allocate(phase.total_compressions * sizeof(int));
+        comp_exp.Allocate(phase.total_compressions * copies * sizeof(int));
+        observation_reads = categorical ? phase.observation_order.size() : 0;
+        observation_order.Upload(phase.observation_order, stream);
+        phase_observations.Allocate(observation_reads * copies);
+        phase.observation_order = {};
         // The records now live on the device; the host keeps the counts.
         phase.rakes = {};
         phase.gathers = {};
         phase.compress = {};
         phase.roots = {};
         schedule = THMM_SCHEDULE_PHASES;
+        SetPhaseRounds(0);
       }
     }
     // Work counters of the forward [0..1] and adjoint [4..5] launches; [2] is
@@ -660,7 +692,7 @@ struct Workspace {
     args.instances = instances.as<DevInstance>();
     args.error = control.as<std::uint32_t>() + 2;
     args.node_in = node_in.ptr;
-    args.observations = observations.as<std::uint8_t>();
+    args.observations = phase_observations.as<std::uint8_t>();
     args.root_potential = root_potential.ptr;
     args.emission = emission.ptr;
     args.categories = static_cast<std::uint32_t>(categories);
@@ -722,6 +754,54 @@ struct Workspace {
     return count;
   }
 
+  // Rounds of the phase schedule run grid-wide (0: the first round with
+  // fewer than 2^17 gathers and compressions); uploads the tail records of
+  // the rest. A tail of more than 2^20 trees stays grid-wide, and so does the
+  // batch layout (every item has every round).
+  void SetPhaseRounds(std::uint32_t rounds) {
+    if (!phase.enabled)
+      return;
+    std::uint32_t wanted = rounds != 0 ? rounds : phase.AutoTailRound(1u << 17);
+    wanted = std::max<std::uint32_t>(wanted, 1);
+    if (phase_batch)
+      wanted = phase.rounds;
+    PhasePlan::Tail tail;
+    if (wanted < phase.rounds) {
+      tail = phase.BuildTail(wanted);
+      if (tail.items.size() > (1u << 20)) {
+        wanted = phase.rounds;
+        tail = PhasePlan::Tail{};
+      }
+    }
+    phase_rounds = std::min(wanted, phase.rounds);
+    tail_instances.clear();
+    for (const Uint4 &item : tail.items)
+      tail_instances.push_back(item.x);
+    tail_items.Upload(tail.items, stream);
+    tail_rounds.Upload(tail.rounds, stream);
+    tail_rakes.Upload(tail.rakes, stream);
+    Check(cudaStreamSynchronize(stream), "tail record upload");
+    DropGraphs();
+  }
+
+  // Rebuilds the phase-ordered observation copy on stream `s` (after the
+  // observations themselves arrived on it).
+  void OrderObservations(cudaStream_t s) {
+    if (phase.enabled && observation_reads != 0)
+      Check(LaunchObservationGather(observations.as<std::uint8_t>(),
+                                    observation_order.as<std::uint32_t>(),
+                                    phase_observations.as<std::uint8_t>(), observation_reads,
+                                    phase_batch ? capacity : 1,
+                                    phase_batch ? observations_per_item : 0, s),
+            "observation ordering launch");
+  }
+  bool UploadsObservations(const std::vector<Upload> &uploads) const {
+    for (const Upload &upload : uploads)
+      if (upload.device == &observations && upload.bytes != 0)
+        return true;
+    return false;
+  }
+
   bool UsePhases(int operation) const {
     return schedule == THMM_SCHEDULE_PHASES && phase.enabled &&
            (operation == THMM_OP_PARTITION || operation == THMM_OP_LOG_PARTITION ||
@@ -749,7 +829,8 @@ struct Workspace {
   // marginals) the adjoint phases in reverse round order. Returns the number
   // of kernel launches.
   int LaunchPhases(int operation, std::uint32_t a, std::uint32_t b) {
-    const PhaseRanges &ranges = PhaseRangesFor(a, b);
+    // Batch layout: every item runs the one tree's operations; items [a, b).
+    const PhaseRanges &ranges = phase_batch ? PhaseRangesFor(0, 1) : PhaseRangesFor(a, b);
     const std::size_t K = states;
     const std::size_t compute_bytes = compute_f64 ? 8 : 4;
     unsigned char *work = scratch.as<unsigned char>();
@@ -759,7 +840,7 @@ struct Workspace {
     args.compress = phase_compress.as<uint4>();
     args.roots = phase_roots.as<uint2>();
     args.node_in = node_in.ptr;
-    args.observations = observations.as<std::uint8_t>();
+    args.observations = phase_observations.as<std::uint8_t>();
     args.root_potential = root_potential.ptr;
     args.emission = emission.ptr;
     args.categories = static_cast<std::uint32_t>(categories);
@@ -769,7 +850,18 @@ struct Workspace {
     args.states = static_cast<std::uint32_t>(states);
     args.nodes = work;
     args.comps = work + total_nodes * K * compute_bytes;
-    args.comp_mu = work + (total_nodes * K + phase.total_compressions * K * K) * compute_bytes;
+    const std::uint64_t copies = phase_batch ? capacity : 1;
+    args.comp_mu =
+        work + (total_nodes * K + phase.total_compressions * copies * K * K) * compute_bytes;
+    if (phase_batch) {
+      args.batch = 1;
+      args.first_item = a;
+      args.items = b - a;
+      args.item_stride = capacity;
+      args.item_nodes = nodes_per_item;
+      args.item_edges = edges_per_item;
+      args.edge_modulus = 0;
+    }
     args.node_exp = node_exp.as<int>();
     args.comp_exp = comp_exp.as<int>();
     args.values = values.ptr;
@@ -777,6 +869,9 @@ struct Workspace {
     args.edge_out = edge_out.ptr;
     args.raw = operation == THMM_OP_PARTITION ? 1u : 0u;
     args.reverse = operation == THMM_OP_MARGINALS ? 1u : 0u;
+    args.tail_items = tail_items.as<uint4>();
+    args.tail_rounds = tail_rounds.as<uint4>();
+    args.tail_rakes = tail_rakes.as<uint2>();
     int count = 0;
     const auto launch = [&](int kind, std::pair<std::uint64_t, std::uint64_t> range) {
       if (range.second <= range.first)
@@ -787,13 +882,23 @@ struct Workspace {
             "tree-HMM accelerator kernel launch");
       ++count;
     };
-    for (std::uint32_t r = 0; r < phase.rounds; ++r) {
+    // Tail trees of instances [a, b).
+    const std::pair<std::uint64_t, std::uint64_t> tail{
+        std::lower_bound(tail_instances.begin(), tail_instances.end(), a) -
+            tail_instances.begin(),
+        std::lower_bound(tail_instances.begin(), tail_instances.end(), b) -
+            tail_instances.begin()};
+    const std::uint32_t grid_rounds = std::min(phase_rounds, phase.rounds);
+    for (std::uint32_t r = 0; r < grid_rounds; ++r) {
       launch(kPhaseGather, ranges.gather[r]);
       launch(kPhaseCompress, ranges.compress[r]);
     }
-    launch(kPhaseFinish, {a, b});
+    launch(kPhaseTailForward, tail);
+    launch(kPhaseFinish, phase_batch ? std::pair<std::uint64_t, std::uint64_t>{0, 1}
+                                     : std::pair<std::uint64_t, std::uint64_t>{a, b});
     if (operation == THMM_OP_MARGINALS) {
-      for (std::uint32_t r = phase.rounds; r-- > 0;) {
+      launch(kPhaseTailReverse, tail);
+      for (std::uint32_t r = grid_rounds; r-- > 0;) {
         launch(kPhaseCompressReverse, ranges.compress[r]);
         launch(kPhaseRakeReverse, ranges.rake[r]);
       }
@@ -929,14 +1034,24 @@ struct Workspace {
         }
       }
     }
-    // The phase schedule has no team or occupancy setting of its own.
+    // The phase schedule's one setting: how many rounds run grid-wide.
     if (phase.enabled && operation != THMM_OP_MAXIMUM && operation != THMM_OP_SAMPLE) {
       schedule = THMM_SCHEDULE_PHASES;
-      const float ms = TimeSteps(operation, repeats);
-      ++tried;
-      if (ms < best.kernel_ms) {
-        best.kernel_ms = ms;
-        best.schedule = THMM_SCHEDULE_PHASES;
+      std::vector<std::uint32_t> tried_rounds;
+      const std::uint32_t automatic = phase.AutoTailRound(1u << 17);
+      for (std::uint32_t rounds : {automatic, 1u, 2u, 3u, 4u, 5u, 6u, 8u, phase.rounds}) {
+        SetPhaseRounds(rounds);
+        if (std::find(tried_rounds.begin(), tried_rounds.end(), phase_rounds) !=
+            tried_rounds.end())
+          continue;
+        tried_rounds.push_back(phase_rounds);
+        const float ms = TimeSteps(operation, repeats);
+        ++tried;
+        if (ms < best.kernel_ms) {
+          best.kernel_ms = ms;
+          best.schedule = THMM_SCHEDULE_PHASES;
+          best.phase_rounds = phase_rounds;
+        }
       }
     }
     best.candidates = tried;
@@ -949,6 +1064,8 @@ struct Workspace {
     if (tuning.schedule != THMM_SCHEDULE_TEAMS && tuning.schedule != THMM_SCHEDULE_PHASES)
       throw std::invalid_argument("unknown schedule");
     schedule = phase.enabled ? tuning.schedule : THMM_SCHEDULE_TEAMS;
+    if (phase.enabled && tuning.phase_rounds != phase_rounds)
+      SetPhaseRounds(tuning.phase_rounds);
     ApplyThreshold(tuning.team_threshold);
     for (int slot = 0; slot < 4; ++slot)
       cta_cap[slot] = static_cast<int>(tuning.ctas_per_sm[slot]);
@@ -964,6 +1081,7 @@ struct Workspace {
     tuning.stripes = stripes_setting;
     tuning.kernel_ms = tuned_ms;
     tuning.schedule = schedule;
+    tuning.phase_rounds = phase_rounds;
     return tuning;
   }
 
@@ -986,6 +1104,8 @@ struct Workspace {
         Check(cudaMemcpyAsync(upload.device->ptr, upload.staging->ptr, upload.bytes,
                               cudaMemcpyHostToDevice, stream),
               "cudaMemcpyAsync input upload");
+    if (UploadsObservations(uploads))
+      OrderObservations(stream);
     Check(cudaEventRecord(events[1], stream), "cudaEventRecord");
     Check(cudaEventRecord(events[2], stream), "cudaEventRecord");
     EnqueueDevice(operation, batch);
@@ -1109,10 +1229,15 @@ struct Workspace {
     const auto host_bytes = [](HostBuffer &buffer) {
       return static_cast<unsigned char *>(buffer.ptr);
     };
+    // With the phase schedule the observations arrive whole with the first
+    // stripe: their phase-ordered copy is rebuilt before any stripe runs.
+    const bool order_observations = UploadsObservations(uploads) && phase.enabled;
     for (std::uint32_t c = 0; c < P; ++c) {
       const Stripe &stripe = stripe_plan[c];
       for (const Upload &upload : uploads) {
-        const auto [offset, size] = SliceRange(upload.slice, upload.unit, upload.bytes,
+        const Slice slice =
+            order_observations && upload.slice == kObservations ? kWhole : upload.slice;
+        const auto [offset, size] = SliceRange(slice, upload.unit, upload.bytes,
                                                stripe.first, stripe.last, c == 0);
         if (size != 0)
           Check(cudaMemcpyAsync(device_bytes(*upload.device) + offset,
@@ -1130,6 +1255,8 @@ struct Workspace {
       Check(cudaStreamWaitEvent(stream, arrived[c], 0), "cudaStreamWaitEvent");
       if (c == 0)
         Check(cudaEventRecord(t[2], stream), "cudaEventRecord");
+      if (c == 0 && order_observations)
+        OrderObservations(stream);
       EngineArgs args = base;
       args.big_items = stripe_order.as<std::uint32_t>() + stripe.first;
       args.big_count = stripe.big;

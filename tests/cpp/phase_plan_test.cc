@@ -4,8 +4,10 @@
 //      compressed path and node value is produced before it is consumed and
 //      consumed exactly once;
 //   2. a double-precision host run of the phase records, launch range by
-//      launch range (whole batch, and cut into instance stripes through
-//      PhasePlan::OpRange), reproduces the oracle's log Z and marginals.
+//      launch range (whole batch, cut into instance stripes through
+//      PhasePlan::OpRange, and with the last rounds taken from the per-tree
+//      tail records), reproduces the oracle's log Z and marginals.
+#include <algorithm>
 #include <cmath>
 #include <cstdint>
 #include <cstdio>
@@ -279,10 +281,12 @@ struct HostRun {
       node_out[(op.y & kMask) * K + m] = mid_adj[m];
   }
 
-  // Runs instances [a, b) the way the runtime launches them.
-  void Run(std::uint32_t a, std::uint32_t b) {
-    using thmm::PhaseKind;
-    for (std::uint32_t r = 0; r < plan.rounds; ++r) {
+  // Runs instances [a, b) the way the runtime launches them: the first
+  // `grid_rounds` rounds as grid-wide phases, the rest from the tail records.
+  void Run(std::uint32_t a, std::uint32_t b, std::uint32_t grid_rounds,
+           const thmm::PhasePlan::Tail &tail) {
+    grid_rounds = std::min(grid_rounds, plan.rounds);
+    for (std::uint32_t r = 0; r < grid_rounds; ++r) {
       const auto g = plan.OpRange(thmm::kPhaseGather, r, a, b);
       for (std::uint64_t i = g.first; i < g.second; ++i)
         Gather(static_cast<std::uint32_t>(i));
@@ -290,9 +294,32 @@ struct HostRun {
       for (std::uint64_t i = c.first; i < c.second; ++i)
         Compress(static_cast<std::uint32_t>(i));
     }
+    for (const thmm::Uint4 &item : tail.items) {
+      if (item.x < a || item.x >= b)
+        continue;
+      for (std::uint32_t e = 0; e < item.z; ++e) {
+        const thmm::Uint4 &round = tail.rounds[item.y + e];
+        for (std::uint32_t i = 0; i < round.y; ++i)
+          Gather(round.x + i);
+        for (std::uint32_t i = 0; i < round.w; ++i)
+          Compress(round.z + i);
+      }
+    }
     for (std::uint32_t i = a; i < b; ++i)
       Finish(i);
-    for (std::uint32_t r = plan.rounds; r-- > 0;) {
+    for (const thmm::Uint4 &item : tail.items) {
+      if (item.x < a || item.x >= b)
+        continue;
+      for (std::uint32_t e = item.z; e-- > 0;) {
+        const thmm::Uint4 &round = tail.rounds[item.y + e];
+        for (std::uint32_t i = 0; i < round.w; ++i)
+          CompressReverse(round.z + i);
+        const thmm::Uint2 &rakes_of = tail.rakes[item.y + e];
+        for (std::uint32_t i = 0; i < rakes_of.y; ++i)
+          RakeReverse(rakes_of.x + i);
+      }
+    }
+    for (std::uint32_t r = grid_rounds; r-- > 0;) {
       const auto c = plan.OpRange(thmm::kPhaseCompress, r, a, b);
       for (std::uint64_t i = c.first; i < c.second; ++i)
         CompressReverse(static_cast<std::uint32_t>(i));
@@ -360,8 +387,12 @@ void CheckForest(std::mt19937_64 &rng, bool shared_edges, std::size_t K, int str
   for (double &v : edge_in)
     v = rng() % 17 == 0 ? 0.0 : u(rng);
 
-  // 2. Host run, whole batch and striped.
-  for (int pass = 0; pass < 2; ++pass) {
+  // 2. Host run: whole batch, striped, and with tails from rounds 1 and 2.
+  for (int pass = 0; pass < 4; ++pass) {
+    const std::uint32_t grid_rounds =
+        pass < 2 ? plan.rounds : static_cast<std::uint32_t>(pass - 1);
+    const thmm::PhasePlan::Tail tail =
+        grid_rounds < plan.rounds ? plan.BuildTail(grid_rounds) : thmm::PhasePlan::Tail{};
     HostRun run{plan, plan.rakes, plan.gathers, plan.compress, plan.roots, K, node_in, edge_in,
                 shared_edges ? static_cast<std::uint32_t>(plans[0].num_edges()) : 0u};
     run.nodes.assign(nodes * K, 0);
@@ -378,7 +409,7 @@ void CheckForest(std::mt19937_64 &rng, bool shared_edges, std::size_t K, int str
     const int parts = pass == 0 ? 1 : stripes;
     for (int s = 0; s < parts; ++s)
       run.Run(static_cast<std::uint32_t>(batch * s / parts),
-              static_cast<std::uint32_t>(batch * (s + 1) / parts));
+              static_cast<std::uint32_t>(batch * (s + 1) / parts), grid_rounds, tail);
     for (std::size_t e = 0; e < edges; ++e)
       EXPECT(run.edge_uses[e] == 1);
     for (std::size_t c = 0; c < comps; ++c)

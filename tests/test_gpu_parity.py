@@ -303,9 +303,14 @@ def test_enqueue_matches_prepared_call(gpu):
     first = ws.posterior_marginals_prepared(
         gpu.BatchedModelView(plan, states, batch, nodes.ravel(), edges))
     values = first.log_partitions.copy()
-    # Phase schedule (the default at K <= 4): gather and compress launches per
-    # round, the finish launch, two adjoint launches per round.
+    # Phase schedule (the default at K <= 4) in the batch API's shared-topology
+    # layout: every round grid-wide (all items have every round, so there is
+    # no per-tree tail whatever phase_rounds asks): gather and compress
+    # launches per round, the finish launch, two adjoint launches per round.
+    assert ws.tuning["phase_rounds"] == plan.num_rounds
     assert plan.num_rounds * 2 + 1 <= ws.launches <= plan.num_rounds * 4 + 1
+    ws.set_tuning(1024, schedule=1, phase_rounds=2)
+    assert ws.tuning["phase_rounds"] == plan.num_rounds
     ws.set_tuning(1024, schedule=0)
     ws.posterior_marginals_prepared(
         gpu.BatchedModelView(plan, states, batch, nodes.ravel(), edges))
@@ -399,3 +404,60 @@ def test_plain_method_configuration(gpu):
         assert np.max(np.abs(view.nodes[n0 * K:(n0 + n) * K] - node_m)) <= 1e-5
         assert np.max(np.abs(view.edges[e0 * K * K:(e0 + e) * K * K] - edge_m)) <= 1e-5
         n0, e0 = n0 + n, e0 + e
+
+
+@pytest.mark.parametrize("categorical", [False, True])
+def test_shared_topology_batch_of_257(gpu, categorical):
+    """The reference's batch API (one plan, B node-factor sets, one shared
+    edge input) at B = 257, more than one block of batch items
+    (tests/accelerator_test.h:24 of the reference): the shared-topology phase
+    layout, where every item reads the one tree's records and the shared
+    edge rows together, against the FP64 oracle, and bit-identical to the
+    per-tree schedule. Dense and categorical inputs, log Z and marginals,
+    and a call on the first 100 items only."""
+    rng = np.random.default_rng(257)
+    K, B = 4, 257
+    parents = synthetic.random_recursive(rng, 400)
+    plan = gpu.Plan(parents)
+    edges = synthetic.stochastic_edges(rng, plan.num_edges, K, 0.7, np.float32)
+    ws = gpu.Workspace()
+    if categorical:
+        observed = synthetic.leaves(parents)
+        ws.reserve_categorical_marginals(plan, K, B, K, observed, scalar=np.float32)
+        staged = ws.categorical_inputs(B)
+        staged.root_potential[:] = rng.random(K) + 0.1
+        staged.emission_potentials[:] = rng.random(K * K) + 0.1
+        staged.edge_potentials[:] = edges
+        staged.observations[:] = rng.integers(0, K, staged.observations.size)
+        model = staged
+        dense = np.ones((B, plan.num_nodes, K), dtype=np.float32)
+        dense[:, plan.root] = staged.root_potential
+        obs = np.array(staged.observations).reshape(B, -1)
+        emission = np.array(staged.emission_potentials).reshape(K, K)
+        dense[:, observed] = dense[:, observed] * emission[obs]
+        dense = dense.astype(np.float64)
+    else:
+        nodes = (rng.random((B, plan.num_nodes, K)) * 0.9 + 0.1).astype(np.float32)
+        model = gpu.BatchedModelView(plan, K, B, nodes.ravel(), edges)
+        dense = nodes.astype(np.float64)
+    assert ws.tuning["schedule"] == 1
+    view = ws.posterior_marginals_prepared(model)
+    got = [np.array(view.log_partitions), np.array(view.nodes), np.array(view.edges)]
+    nodes_out = got[1].reshape(B, -1)
+    edges_out = got[2].reshape(B, -1)
+    for b in range(0, B, 16):
+        log_z, _, node_m, edge_m = bridge.marginals(plan, K, dense[b].ravel(),
+                                                    edges.astype(np.float64))
+        assert abs(got[0][b] - log_z) <= 1e-6 * max(1.0, abs(log_z))
+        assert np.max(np.abs(nodes_out[b] - node_m)) <= 1e-5
+        assert np.max(np.abs(edges_out[b] - edge_m)) <= 1e-5
+    ws.set_tuning(1024, schedule=0)
+    teams = ws.posterior_marginals_prepared(model)
+    assert np.array_equal(np.array(teams.log_partitions), got[0])
+    assert np.array_equal(np.array(teams.nodes), got[1])
+    assert np.array_equal(np.array(teams.edges), got[2])
+    if not categorical:
+        ws.set_tuning(1024, schedule=1)
+        part = ws.log_partition_function_prepared(
+            gpu.BatchedModelView(plan, K, 100, nodes[:100].ravel(), edges))
+        assert np.array_equal(np.array(part.values), got[0][:100])

@@ -5,7 +5,8 @@ the CTAs per SM of each kernel and CUDA-graph replay of the device-only step
 only move work between SMs, CTAs and warps; the phase schedule (every round
 of every tree in one grid-wide launch, K <= 4) performs each operation's
 arithmetic in the same order and carries the power-of-two exponents with the
-stored values instead of per team. Every operation's floating-point result
+stored values instead of per team, whichever rounds run grid-wide and which
+run in one warp per tree. Every operation's floating-point result
 and the integer exponent sums are the same, so every output must be
 bit-identical across all of them.
 """
@@ -49,9 +50,10 @@ def test_tunings_give_identical_marginals(gpu, states):
                 (1 << 31, (0, 0, 0, 0)),    # every tree to a warp team
                 (1000, (1, 0, 0, 1)),       # one CTA per SM for both sweeps
                 (300, (2, 0, 0, 3))]
-    for schedule in (TEAMS, PHASES):
+    for schedule, phase_rounds in ((TEAMS, 0), (PHASES, 0), (PHASES, 1), (PHASES, 3),
+                                   (PHASES, 99)):
         for threshold, caps in settings:
-            ws.set_tuning(threshold, caps, schedule=schedule)
+            ws.set_tuning(threshold, caps, schedule=schedule, phase_rounds=phase_rounds)
             assert ws.tuning["team_threshold"] == threshold
             assert ws.tuning["ctas_per_sm"] == list(caps)
             assert ws.tuning["schedule"] == (schedule if states <= 4 else TEAMS)
@@ -74,7 +76,8 @@ def test_graph_replay_matches_prepared_call(gpu, schedule):
     plans, nodes, edges = forest(gpu, rng, 4)
     ws = gpu.Workspace()
     ws.reserve_forest(plans, 4, kind="marginals", scalar=np.float32)
-    ws.set_tuning(1024, schedule=schedule)
+    rounds = max(p.num_rounds for p in plans)
+    ws.set_tuning(1024, schedule=schedule, phase_rounds=rounds)
     model = gpu.BatchedModelView(None, 4, len(plans), nodes, edges)
     reference = outputs(ws.posterior_marginals_prepared(model))
     staged = ws.inputs()
@@ -85,8 +88,14 @@ def test_graph_replay_matches_prepared_call(gpu, schedule):
     if schedule == TEAMS:
         assert ws.launches == 2
     else:  # gather + compress per round, finish, two adjoint phases per round
-        rounds = max(p.num_rounds for p in plans)
         assert 2 * rounds + 1 <= ws.launches <= 4 * rounds + 1
+        # Two grid-wide rounds, then one warp per tree: two tail launches.
+        ws.set_tuning(1024, schedule=schedule, phase_rounds=2)
+        assert ws.tuning["phase_rounds"] == 2
+        ws.enqueue(4)
+        ws.synchronize()
+        assert 2 * 2 + 3 <= ws.launches <= 2 * 4 + 3
+        ws.set_tuning(1024, schedule=schedule, phase_rounds=rounds)
     # Outputs of the replays are in device memory; a kNone-style rerun through
     # the prepared call downloads the same values.
     got = outputs(ws.posterior_marginals_prepared(
