@@ -692,7 +692,7 @@ struct Workspace {
     args.instances = instances.as<DevInstance>();
     args.error = control.as<std::uint32_t>() + 2;
     args.node_in = node_in.ptr;
-    args.observations = phase_observations.as<std::uint8_t>();
+    args.observations = observations.as<std::uint8_t>();
     args.root_potential = root_potential.ptr;
     args.emission = emission.ptr;
     args.categories = static_cast<std::uint32_t>(categories);
