@@ -437,6 +437,7 @@ def test_shared_topology_batch_of_257(gpu, categorical):
         dense[:, observed] = dense[:, observed] * emission[obs]
         dense = dense.astype(np.float64)
     else:
+        ws.reserve_marginals(plan, K, B, scalar=np.float32)
         nodes = (rng.random((B, plan.num_nodes, K)) * 0.9 + 0.1).astype(np.float32)
         model = gpu.BatchedModelView(plan, K, B, nodes.ravel(), edges)
         dense = nodes.astype(np.float64)
