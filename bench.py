@@ -68,6 +68,8 @@ def parse_args():
     parser.add_argument("--seed", type=int, default=0)
     parser.add_argument("--e2e-steps", type=int, default=None)
     parser.add_argument("--cpu-sample-nodes", type=int, default=20_000_000)
+    parser.add_argument("--precision", choices=["tf32x3", "bf16"], default="tf32x3",
+                        help="dense workload above 32 states: tensor-core product tier")
     parser.add_argument("--check-trees", type=int, default=16,
                         help="gw workload: trees checked against the oracle")
     parser.add_argument("--workload", choices=["forest", "gw", "dense"], default="forest",
@@ -870,11 +872,13 @@ def run_dense(args, rank, world, local_rank, dist):
         edge_chunks(keep)
         rng.bit_generator.state = state
 
+        oracle_results = {}
+
         def job(t):
-            bridge.marginals(plans[t], K,
-                             node_factors[node0[t] * K:node0[t + 1] * K].astype(np.float64),
-                             sample_edges[edge0[t] * K * K:edge0[t + 1] * K * K]
-                             .astype(np.float64))
+            log_z, _, node_m, _ = bridge.marginals(
+                plans[t], K, node_factors[node0[t] * K:node0[t + 1] * K].astype(np.float64),
+                sample_edges[edge0[t] * K * K:edge0[t + 1] * K * K].astype(np.float64))
+            oracle_results[t] = (log_z, node_m)
             return plans[t].num_nodes
 
         start = time.perf_counter()
@@ -896,13 +900,15 @@ def run_dense(args, rank, world, local_rank, dist):
             return
     else:
         cpu = None
+        oracle_results = {}
 
     import torch
 
     device = local_rank
     torch.cuda.set_device(device)
     ws = thmm.Workspace()
-    ws.reserve_forest(plans, K, device, kind="marginals", scalar=np.float32)
+    ws.reserve_forest(plans, K, device, kind="marginals", scalar=np.float32,
+                      compute="bf16" if args.precision == "bf16" else None)
     staged = ws.inputs()
     staged.node_potentials[:] = node_factors
 
@@ -914,6 +920,17 @@ def run_dense(args, rank, world, local_rank, dist):
     finite = bool(np.all(np.isfinite(first.log_partitions)))
     node_sum_error = float(np.max(np.abs(
         np.array(first.nodes).reshape(-1, K).sum(axis=1) - 1.0)))
+    # Errors against the FP64 oracle on the CPU leg's sample trees.
+    accuracy = {}
+    if oracle_results:
+        got_nodes = np.array(first.nodes)
+        rel, worst = 0.0, 0.0
+        for t, (log_z, node_m) in oracle_results.items():
+            rel = max(rel, abs(float(first.log_partitions[t]) - log_z) / max(1.0, abs(log_z)))
+            worst = max(worst, float(np.max(np.abs(
+                got_nodes[node0[t] * K:node0[t + 1] * K] - node_m))))
+        accuracy = {"checked_trees": len(oracle_results), "log_z_max_rel_error": rel,
+                    "node_marginal_max_abs_error": worst}
 
     ext = torch.cuda.ExternalStream(ws.stream, device=device)
     for _ in range(args.warmup):
@@ -955,9 +972,11 @@ def run_dense(args, rank, world, local_rank, dist):
         "metric": metric, "value": value, "unit": UNIT, "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": step_ms,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-        "dtype": "f32 (3xTF32 tensor-core products)" if K > 32 else "f32",
+        "dtype": ("f32" if K <= 32 else "f32 (BF16 tensor-core products)"
+                  if args.precision == "bf16" else "f32 (3xTF32 tensor-core products)"),
         "data": "synthetic",
-        "config": {**config, "all_log_z_finite": finite,
+        "config": {**config, "all_log_z_finite": finite, "precision_tier": args.precision,
+                   "accuracy_vs_fp64_oracle": accuracy,
                    "node_marginal_normalisation_error": node_sum_error,
                    ("useful_tensor_tflops" if K > 32 else "useful_product_tflops"):
                        useful_flops / (step_ms / 1e3) / 1e12},

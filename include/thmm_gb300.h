@@ -55,6 +55,12 @@ enum {
    * marginals) in FP64 instead of the default FP32 with exact power-of-two
    * scaling. MAP and sampling always compute in the scalar width. */
   THMM_COMPUTE_F64 = 0x100u,
+  /* Extension: the BF16 tier of the tensor-core engine (more than 32 states):
+   * compress products and their adjoint products in one pass of BF16
+   * operands with FP32 accumulation, instead of the default 3xTF32 (FP32
+   * accuracy). About 8 significant bits per operand: faster tensor-core
+   * work, looser results (measured errors are stated in the design doc). */
+  THMM_COMPUTE_BF16 = 0x200u,
 };
 
 /* tree_hmm::CategoricalInputUpdate (include/tree_hmm/accelerator.h:89-93). */

@@ -32,6 +32,7 @@ THMM_RESERVE_MAXIMUM = 1
 THMM_RESERVE_SAMPLING = 2
 THMM_RESERVE_MARGINALS = 4
 THMM_COMPUTE_F64 = 0x100
+THMM_COMPUTE_BF16 = 0x200
 THMM_UPDATE_ALL = 0
 THMM_UPDATE_FACTORS = 1
 THMM_UPDATE_NONE = 2

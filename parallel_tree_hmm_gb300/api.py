@@ -256,7 +256,9 @@ class Workspace:
         flags = 0
         for part in kind.split(","):  # e.g. "maximum,sampling"
             flags |= table[part.strip()]
-        if compute is not None and np.dtype(compute) == np.float64:
+        if isinstance(compute, str) and compute == "bf16":
+            flags |= _lib.THMM_COMPUTE_BF16  # BF16 tier of the tensor-core engine
+        elif compute is not None and np.dtype(compute) == np.float64:
             flags |= _lib.THMM_COMPUTE_F64
         return flags
 

@@ -135,6 +135,7 @@ struct EngineArgs {
   void *edge_out; // edge marginals
   std::uint32_t *states_out;
   const void *uniforms;
+  std::uint32_t bf16; // wide-state engine: BF16 tensor products (the BF16 tier)
 };
 
 // Scratch sizes of one instance, in compute elements and bytes.

@@ -130,6 +130,7 @@ struct Workspace {
   int device = 0;
   int scalar = THMM_SCALAR_F64;
   bool compute_f64 = false;
+  bool bf16 = false; // BF16 tier of the tensor-core engine
   bool maximum = false;
   bool sampling = false;
   bool marginals = false;
@@ -337,6 +338,9 @@ struct Workspace {
          (flags & (THMM_RESERVE_MAXIMUM | THMM_RESERVE_SAMPLING)) != 0))
       throw std::invalid_argument(
           "state counts above 32 support FP32 log partitions and marginals only");
+    if ((flags & THMM_COMPUTE_BF16) != 0 && state_count <= 32)
+      throw std::invalid_argument(
+          "BF16 tensor products are a tier of the tensor-core engine (more than 32 states)");
     Clear();
     device = device_index;
     Check(cudaSetDevice(device), "cudaSetDevice");
@@ -361,6 +365,7 @@ struct Workspace {
     states = state_count;
     scalar = static_cast<int>(scalar_bytes);
     compute_f64 = (flags & THMM_COMPUTE_F64) != 0;
+    bf16 = (flags & THMM_COMPUTE_BF16) != 0;
     maximum = (flags & THMM_RESERVE_MAXIMUM) != 0;
     sampling = (flags & THMM_RESERVE_SAMPLING) != 0;
     marginals = (flags & THMM_RESERVE_MARGINALS) != 0;
@@ -708,6 +713,7 @@ struct Workspace {
     args.edge_out = edge_out.ptr;
     args.states_out = states_out.as<std::uint32_t>();
     args.uniforms = uniforms.ptr;
+    args.bf16 = bf16 ? 1u : 0u;
     return args;
   }
 

@@ -3,7 +3,7 @@
 // shared memory, completion through an mbarrier, and accumulator read-back.
 //
 // Operand layout: no swizzle, K-major "core matrices" of 8 rows x 16 bytes
-// (8 x 4 fp32 values), 128 contiguous bytes each. Element (row, k) of an
+// (8 x 4 fp32 values, or 8 x 8 bf16 values), 128 contiguous bytes each. Element (row, k) of an
 // operand lives at
 //     (row / 8) * SBO + (k / 4) * LBO + (row % 8) * 16 + (k % 4) * 4
 // with LBO (the byte distance between core matrices adjacent in K) = 128 and
@@ -49,6 +49,12 @@ __host__ __device__ constexpr std::uint32_t Tf32Descriptor(unsigned m, unsigned 
   return (1u << 4) | (2u << 7) | (2u << 10) | ((n >> 3) << 17) | ((m >> 4) << 24);
 }
 
+// Instruction descriptor of kind::f16 with BF16 A and B (the same type for
+// both, as kind::f16 requires), FP32 accumulator, both K-major, M x N tile.
+__host__ __device__ constexpr std::uint32_t Bf16Descriptor(unsigned m, unsigned n) {
+  return (1u << 4) | (1u << 7) | (1u << 10) | ((n >> 3) << 17) | ((m >> 4) << 24);
+}
+
 // Allocates `columns` (power of two, >= 32) TMEM columns; the base address is
 // written to `*slot` (shared memory). Executed by one whole warp.
 __device__ __forceinline__ void Allocate(std::uint32_t *slot, std::uint32_t columns) {
@@ -89,6 +95,16 @@ __device__ __forceinline__ void MmaTf32(std::uint32_t tmem, std::uint64_t a,
                                         bool accumulate) {
   asm volatile("{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
                " tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n}" ::"r"(tmem),
+               "l"(a), "l"(b), "r"(idesc), "r"(accumulate ? 1u : 0u)
+               : "memory");
+}
+
+// D[tmem] (+)= A * B for one depth-16 slice of BF16 operands.
+__device__ __forceinline__ void MmaBf16(std::uint32_t tmem, std::uint64_t a,
+                                        std::uint64_t b, std::uint32_t idesc,
+                                        bool accumulate) {
+  asm volatile("{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+               " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}" ::"r"(tmem),
                "l"(a), "l"(b), "r"(idesc), "r"(accumulate ? 1u : 0u)
                : "memory");
 }

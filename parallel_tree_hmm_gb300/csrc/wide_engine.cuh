@@ -25,6 +25,7 @@
 
 #include <cstdint>
 #include <type_traits>
+#include <cuda_bf16.h>
 #include <cuda_runtime.h>
 
 #include "engine.cuh"
@@ -196,6 +197,58 @@ __device__ __forceinline__ void Stage(const Source &src, unsigned K, unsigned d0
   }
 }
 
+// BF16 tier: the same operands as single BF16 values (round to nearest
+// even), K-major core matrices of 8 rows x 8 values. Element (row, k) of a
+// depth chunk sits at (row / 8) * kSbo16 + (k / 8) * 128 + (row % 8) * 16 +
+// (k % 8) * 2 in the hi buffer of the operand; one kind::f16 MMA consumes a
+// depth of 16 (two core matrices), so step k starts 256 bytes further.
+constexpr std::uint32_t kSbo16 = kChunk / 8 * 128; // 1024 bytes between 8-row groups
+
+__device__ __forceinline__ std::uint32_t CoreOffset16(unsigned row, unsigned k) {
+  return (row / 8) * kSbo16 + (k / 8) * 128u + (row % 8) * 16u + (k % 8) * 2u;
+}
+
+__device__ __forceinline__ unsigned short Bf16Bits(float v) {
+  return __bfloat16_as_ushort(__float2bfloat16_rn(v));
+}
+
+template <class Source>
+__device__ __forceinline__ void StageBf16(const Source &src, unsigned K, unsigned d0,
+                                          unsigned char *dst) {
+  const unsigned depth = K > d0 ? (K - d0 < kChunk ? K - d0 : kChunk) : 0u;
+  if (d0 != 0 && depth < kChunk) {
+    // A later chunk: clear depths [depth, kChunk) left over from the first.
+    const unsigned pad = kChunk - depth;
+    for (unsigned idx = threadIdx.x; idx < K * pad; idx += kThreads)
+      *reinterpret_cast<unsigned short *>(dst + CoreOffset16(idx / pad, depth + idx % pad)) = 0;
+  }
+  if constexpr (std::is_same_v<Source, RowMajor>) {
+    if (K % 4 == 0) {
+      const unsigned quads = depth / 4;
+#pragma unroll 4
+      for (unsigned idx = threadIdx.x; idx < K * quads; idx += kThreads) {
+        const unsigned r = idx / quads, q = idx % quads;
+        const float4 v = src.Quad(K, r, d0 + 4 * q);
+        const uint2 packed = make_uint2(Bf16Bits(v.x) | (unsigned(Bf16Bits(v.y)) << 16),
+                                        Bf16Bits(v.z) | (unsigned(Bf16Bits(v.w)) << 16));
+        *reinterpret_cast<uint2 *>(dst + CoreOffset16(r, 4 * q)) = packed;
+      }
+      return;
+    }
+#pragma unroll 4
+    for (unsigned idx = threadIdx.x; idx < K * depth; idx += kThreads) {
+      const unsigned r = idx / depth, d = idx % depth;
+      *reinterpret_cast<unsigned short *>(dst + CoreOffset16(r, d)) = Bf16Bits(src(K, r, d0 + d));
+    }
+  } else {
+#pragma unroll 4
+    for (unsigned idx = threadIdx.x; idx < K * depth; idx += kThreads) {
+      const unsigned r = idx % K, d = idx / K;
+      *reinterpret_cast<unsigned short *>(dst + CoreOffset16(r, d)) = Bf16Bits(src(K, r, d0 + d));
+    }
+  }
+}
+
 // Clears the four operand buffers (once per launch).
 template <int KP> __device__ __forceinline__ void ClearOperands(unsigned char *smem) {
   float4 *p = reinterpret_cast<float4 *>(smem);
@@ -215,9 +268,14 @@ template <int KP> __device__ __forceinline__ void ClearOperands(unsigned char *s
 // takes at most 16 tensor-core steps instead of 48 at K = 128, and the
 // tensor core's accumulation error grows with the steps accumulated into one
 // accumulator (about 1.7e-6 relative on log Z at K = 128 with one).
+//
+// With `bf16` (the BF16 tier, a workspace-wide choice) each product is one
+// pass of BF16 operands instead (kind::f16, FP32 accumulation, one
+// accumulator whatever kSplit asks): about 8 significant bits per operand.
 template <int KP, class XS, class YS, bool kSplit = false>
 __device__ bool Product(unsigned char *smem, Shared &sh, std::uint32_t &phase,
-                        std::uint32_t tmem, unsigned K, const XS &x, const YS &y) {
+                        std::uint32_t tmem, unsigned K, const XS &x, const YS &y,
+                        bool bf16) {
   static_assert(KP % kChunk == 0 && KP <= 128, "padded state count");
   unsigned char *const xh = smem + Layout<KP>::kXh;
   unsigned char *const xl = smem + Layout<KP>::kXl;
@@ -225,6 +283,31 @@ __device__ bool Product(unsigned char *smem, Shared &sh, std::uint32_t &phase,
   unsigned char *const yl = smem + Layout<KP>::kYl;
   constexpr std::uint32_t kDescriptor = umma::Tf32Descriptor(128, KP);
   bool ok = true;
+  if (bf16) {
+    constexpr std::uint32_t kBf16 = umma::Bf16Descriptor(128, KP);
+#pragma unroll 1
+    for (unsigned chunk = 0; chunk < KP / kChunk; ++chunk) {
+      StageBf16(x, K, chunk * kChunk, xh);
+      StageBf16(y, K, chunk * kChunk, yh);
+      umma::FenceOperands();
+      umma::FenceBeforeSync();
+      __syncthreads();
+      umma::FenceAfterSync();
+      if (threadIdx.x == 0) {
+        const std::uint32_t xh_at = umma::SmemAddress(xh), yh_at = umma::SmemAddress(yh);
+#pragma unroll
+        for (unsigned k = 0; k < kChunk / 16; ++k)
+          umma::MmaBf16(tmem, umma::SmemDescriptor(xh_at + k * 256, kSbo16),
+                        umma::SmemDescriptor(yh_at + k * 256, kSbo16), kBf16,
+                        chunk != 0 || k != 0);
+        umma::Commit(&sh.barrier);
+      }
+      ok = umma::Wait(&sh.barrier, phase) && ok;
+      phase ^= 1u;
+      umma::FenceAfterSync();
+    }
+    return ok;
+  }
 #pragma unroll 1
   for (unsigned chunk = 0; chunk < KP / kChunk; ++chunk) {
     const unsigned d0 = chunk * kChunk;
@@ -269,8 +352,10 @@ __device__ bool Product(unsigned char *smem, Shared &sh, std::uint32_t &phase,
 // then the small-part accumulator, added in FP32.
 template <int KP>
 __device__ __forceinline__ void SplitSum32(std::uint32_t lane_base, unsigned c,
-                                           float (&row)[32]) {
+                                           float (&row)[32], bool bf16) {
   umma::Load32(lane_base + c, row);
+  if (bf16)
+    return; // the BF16 tier keeps one accumulator
 #pragma unroll 1
   for (unsigned part = 1; part <= KP / kChunk; ++part) {
     float more[32];

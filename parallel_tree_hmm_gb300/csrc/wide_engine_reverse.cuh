@@ -108,7 +108,7 @@ template <int KP> __device__ void Tree<KP>::Reverse() {
         const float *mid = middle;
         // Unnormalised output, recomputed: left * diag(middle) * right.
         ok = Product<KP>(smem, sh, phase, tmem + Layout<KP>::kProductColumn, K,
-                         RowMajor{left, middle}, Transposed{right}) &&
+                         RowMajor{left, middle}, Transposed{right}, a.bf16 != 0) &&
              ok;
         // ratio = adjoint / output, written over the output adjoint (each
         // path version's adjoint is read only here).
@@ -134,11 +134,12 @@ template <int KP> __device__ void Tree<KP>::Reverse() {
         const float *ratio_matrix = output_adjoint;
         // P1[r][m] = sum_c ratio[r][c] right[m][c]  (left adjoint factor).
         ok = Product<KP>(smem, sh, phase, tmem + Layout<KP>::kLeftColumn, K,
-                         RowMajor{ratio_matrix, nullptr}, RowMajor{right, nullptr}) &&
+                         RowMajor{ratio_matrix, nullptr}, RowMajor{right, nullptr},
+                         a.bf16 != 0) &&
              ok;
         // P2[m][c] = sum_r left[r][m] ratio[r][c]  (right adjoint factor).
         ok = Product<KP>(smem, sh, phase, tmem + Layout<KP>::kRightColumn, K, Transposed{left},
-                         Transposed{ratio_matrix}) &&
+                         Transposed{ratio_matrix}, a.bf16 != 0) &&
              ok;
         // Row j: left adjoint left[j][m] middle[m] P1[j][m]; right adjoint
         // right[j][c] middle[j] P2[j][c]; middle adjoint sum_c of the latter.

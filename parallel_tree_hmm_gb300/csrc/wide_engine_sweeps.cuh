@@ -79,7 +79,7 @@ template <int KP> __device__ void Tree<KP>::Forward() {
         ok = Product<KP, RowMajor, Transposed, true>(smem, sh, phase,
                                                      tmem + Layout<KP>::kProductColumn, K,
                                                      RowMajor{left, middle},
-                                                     Transposed{right}) &&
+                                                     Transposed{right}, a.bf16 != 0) &&
              ok;
         // Row j of the product is tensor-memory lane j: maximum, then scale.
         const std::uint32_t lane_base =
@@ -88,7 +88,7 @@ template <int KP> __device__ void Tree<KP>::Forward() {
 #pragma unroll 1
         for (unsigned c = 0; c < KP; c += 32) {
           float row[32];
-          SplitSum32<KP>(lane_base, c, row);
+          SplitSum32<KP>(lane_base, c, row, a.bf16 != 0);
 #pragma unroll
           for (unsigned q = 0; q < 32; ++q)
             if (j < K && c + q < K)
@@ -99,7 +99,7 @@ template <int KP> __device__ void Tree<KP>::Forward() {
 #pragma unroll 1
         for (unsigned c = 0; c < KP; c += 32) {
           float row[32];
-          SplitSum32<KP>(lane_base, c, row);
+          SplitSum32<KP>(lane_base, c, row, a.bf16 != 0);
 #pragma unroll
           for (unsigned q = 0; q < 32; ++q)
             if (j < K && c + q < K)

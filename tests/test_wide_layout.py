@@ -68,3 +68,47 @@ def test_instruction_descriptor_fields():
         assert (d >> 15) & 3 == 0          # both K-major
         assert ((d >> 17) & 63) << 3 == n
         assert ((d >> 24) & 31) << 4 == 128
+
+
+# BF16 tier: the same buffers hold one BF16 operand in 8-row x 8-value core
+# matrices (csrc/wide_engine.cuh CoreOffset16); one kind::f16 MMA reads a
+# depth of 16 (two core matrices), so depth step k starts 256 bytes further.
+SBO16 = CHUNK // 8 * 128
+
+
+def core_offset16(row, k):
+    return (row // 8) * SBO16 + (k // 8) * LBO + (row % 8) * 16 + (k % 8) * 2
+
+
+@pytest.mark.parametrize("kp", [64, 128])
+def test_bf16_operand_and_descriptor_bounds(kp):
+    L = layout(kp)
+    for rows, size in ((128, L["x_bytes"]), (kp, L["y_bytes"])):
+        offsets = [core_offset16(r, d) for r in range(rows) for d in range(CHUNK)]
+        # Every element in its own two bytes, inside the operand's hi buffer.
+        assert len(set(offsets)) == len(offsets)
+        assert max(offsets) + 2 <= size
+        for k in range(CHUNK // 16):
+            start = k * 2 * LBO
+            last = start + LBO + (rows // 8 - 1) * SBO16 + 127
+            assert last < size
+    # A quad of depths 4q..4q+3 is 8 contiguous, 8-byte-aligned bytes.
+    for r in range(0, kp, 7):
+        for q in range(CHUNK // 4):
+            base = core_offset16(r, 4 * q)
+            assert base % 8 == 0
+            assert [core_offset16(r, 4 * q + i) for i in range(4)] == [base + 2 * i
+                                                                     for i in range(4)]
+
+
+def test_bf16_instruction_descriptor_fields():
+    def bf16_descriptor(m, n):
+        return (1 << 4) | (1 << 7) | (1 << 10) | ((n >> 3) << 17) | ((m >> 4) << 24)
+
+    for n in (64, 128):
+        d = bf16_descriptor(128, n)
+        assert (d >> 4) & 3 == 1                          # FP32 accumulator
+        assert (d >> 7) & 7 == 1 and (d >> 10) & 7 == 1   # BF16 A and B (same type)
+        assert (d >> 15) & 3 == 0
+        assert ((d >> 17) & 63) << 3 == n
+        assert ((d >> 24) & 31) << 4 == 128
