@@ -68,6 +68,9 @@ def parse_args():
     parser.add_argument("--seed", type=int, default=0)
     parser.add_argument("--e2e-steps", type=int, default=None)
     parser.add_argument("--cpu-sample-nodes", type=int, default=20_000_000)
+    parser.add_argument("--windows", type=int, default=1,
+                        help="dense workload: stream the trees through the device in this "
+                             "many windows, inputs drawn on the GPU (full-size runs)")
     parser.add_argument("--precision", choices=["tf32x3", "bf16"], default="tf32x3",
                         help="dense workload above 32 states: tensor-core product tier")
     parser.add_argument("--check-trees", type=int, default=16,
@@ -826,6 +829,9 @@ def run_dense(args, rank, world, local_rank, dist):
     rng = np.random.default_rng(rank_seed(args.seed, rank))
     grow = synthetic.spine_heavy if args.shape == "spine-heavy" else synthetic.random_recursive
     parents = [grow(rng, args.tree_nodes) for _ in range(args.trees)]
+    if args.windows > 1 and args.impl == "ours":
+        run_dense_streamed(args, rank, world, local_rank, dist, parents)
+        return
     # The reference arm plans with the oracle's planner library (no product
     # code loaded); the same planner source gives the same plans.
     plans = ([bridge.CpuPlan(p) for p in parents] if args.impl == "reference"
@@ -989,6 +995,133 @@ def run_dense(args, rank, world, local_rank, dist):
                 "d2h_bytes_per_step": (total_edges * K * K + total_nodes * K) * S
                 + len(plans) * S + 16},
         "gpu_launches": 2 * args.steps,
+        "clocks": sampler.summary(),
+    }
+    if cpu is not None:
+        line["cpu_baseline"] = cpu
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+
+
+def run_dense_streamed(args, rank, world, local_rank, dist, parents):
+    """The dense workload at a size beyond HBM: the trees pass through one
+    workspace in `args.windows` windows. Each window's node and edge factors
+    are drawn on the GPU straight into the workspace's device buffers
+    (device_buffers, device_inputs_ready) and contracted by the device-only
+    step; the value is all nodes over the summed device time of the windows'
+    steps. Accuracy is covered by the scaled runs of the same laws and by the
+    streamed-window parity tests; the CPU baseline is the FP64 oracle on one
+    2,000-node tree of the same laws (K <= 64)."""
+    import torch
+
+    import parallel_tree_hmm_gb300 as thmm
+    from oracle import bridge
+
+    K = args.states
+    device = local_rank
+    torch.cuda.set_device(device)
+    generator = torch.Generator(device=f"cuda:{device}")
+    generator.manual_seed(rank_seed(args.seed, rank))
+    bounds = np.linspace(0, len(parents), args.windows + 1).astype(int)
+    ws = thmm.Workspace()
+    window_ms, nodes_done, compressions = [], 0, 0
+    finite, node_sum_error, cpu, launches = True, 0.0, None, 0
+    sampler = ClockSampler(device)
+
+    def fill(view, sigma, zero_fraction):
+        chunk = 1 << 26
+        for start in range(0, view.numel(), chunk):
+            n = min(chunk, view.numel() - start)
+            x = torch.randn(n, generator=generator, device=view.device)
+            x.mul_(sigma).exp_()
+            if zero_fraction > 0:
+                x[torch.rand(n, generator=generator, device=view.device) < zero_fraction] = 0
+            view[start:start + n].copy_(x)
+
+    with sampler:
+        for w in range(args.windows):
+            plans = thmm.Plan.many(parents[bounds[w]:bounds[w + 1]])
+            ws.reserve_forest(plans, K, device, kind="marginals,device", scalar=np.float32,
+                              compute="bf16" if args.precision == "bf16" else None)
+            buffers = ws.device_buffers()
+            fill(buffers["node_potentials"], 1.0, 0.0)
+            fill(buffers["edge_potentials"], args.edge_sigma, args.zero_fraction)
+            torch.cuda.synchronize(device)
+            ws.device_inputs_ready()
+            ext = torch.cuda.ExternalStream(ws.stream, device=device)
+            ws.enqueue(4)  # untimed: captures the step's CUDA graph
+            begin = torch.cuda.Event(enable_timing=True)
+            end = torch.cuda.Event(enable_timing=True)
+            begin.record(ext)
+            nodes_done += ws.enqueue(4)
+            end.record(ext)
+            end.synchronize()
+            launches += ws.launches
+            window_ms.append(begin.elapsed_time(end))
+            compressions += sum(int(p.num_compressions) for p in plans)
+            log_z = buffers["values"].cpu().numpy()
+            finite = finite and bool(np.all(np.isfinite(log_z)))
+            node_sum_error = max(node_sum_error, float(
+                (buffers["node_marginals"].view(-1, K).sum(dim=1) - 1).abs().max()))
+            if w == 0 and rank == 0 and K <= 64 and args.cpu_sample_nodes > 0:
+                # A 100,000-node tree takes the FP64 oracle minutes, so the CPU
+                # sample is one 2,000-node tree of the same shape and factor laws.
+                from parallel_tree_hmm_gb300 import synthetic
+
+                sample_rng = np.random.default_rng(rank_seed(args.seed, rank) + 7)
+                grow = (synthetic.spine_heavy if args.shape == "spine-heavy"
+                        else synthetic.random_recursive)
+                plan = bridge.CpuPlan(grow(sample_rng, 2000))
+                n, e = plan.num_nodes, plan.num_edges
+                nodes = np.exp(sample_rng.standard_normal(n * K))
+                edges = np.exp(args.edge_sigma * sample_rng.standard_normal(e * K * K))
+                edges[sample_rng.random(e * K * K) < args.zero_fraction] = 0.0
+                start = time.perf_counter()
+                bridge.marginals(plan, K, nodes, edges)
+                elapsed = time.perf_counter() - start
+                cpu = {"value": n / elapsed, "unit": UNIT, "cores": 1, "kind": "port",
+                       "sample": f"one {n}-node tree of the same laws, FP64 log-domain "
+                                 f"marginals, {elapsed:.1f} s on one core"}
+            del buffers
+    total_ms = reduce_max(sum(window_ms), dist)
+    total_nodes = sum(len(p) for p in parents)
+    total_edges = total_nodes - len(parents)
+    value = nodes_done * world / (total_ms / 1e3)
+    S = 4
+    algorithmic = 2 * total_edges * K * K * S + 2 * total_nodes * K * S + len(parents) * S
+    peaks = json.loads((ROOT / "MEASURED_PEAKS.json").read_text()) \
+        if (ROOT / "MEASURED_PEAKS.json").exists() else {}
+    peak = peaks.get("hbm_gbs", 6800.0)
+    line = {
+        "metric": "tree-nodes/s for logZ+marginals+grad (dense factors)", "value": value,
+        "unit": UNIT, "n_gpus": world, "steps": 1, "warmup": 1,
+        "ms_per_step": total_ms, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": ("f32 (BF16 tensor-core products)" if args.precision == "bf16"
+                  else "f32 (3xTF32 tensor-core products)") if K > 32 else "f32",
+        "data": "synthetic, drawn on the GPU",
+        "config": {"workload": (f"dense factors at full size: {len(parents)} {args.shape} trees "
+                                f"of {args.tree_nodes} nodes, K={K}, lognormal(0,1) node and "
+                                f"lognormal(0,{args.edge_sigma:g}) edge factors with "
+                                f"{100 * args.zero_fraction:g}% zeros, marginals"),
+                   "trees": len(parents), "nodes_per_rank": total_nodes, "states": K,
+                   "windows": args.windows, "window_ms": [round(v, 2) for v in window_ms],
+                   "edge_factor_bytes": total_edges * K * K * S,
+                   "compressions_per_rank": compressions, "precision_tier": args.precision,
+                   "all_log_z_finite": finite,
+                   "node_marginal_normalisation_error": node_sum_error,
+                   ("useful_tensor_tflops" if K > 32 else "useful_product_tflops"):
+                       4 * 2 * compressions * K ** 3 / (total_ms / 1e3) / 1e12,
+                   "l2": "inputs larger than L2"},
+        "roofline": {"bound": "hbm", "achieved": algorithmic / (total_ms / 1e3) / 1e9,
+                     "peak": peak, "unit": "GB/s",
+                     "frac": algorithmic / (total_ms / 1e3) / 1e9 / peak,
+                     "peak_source": "measured" if peaks else "fallback", "traffic": None,
+                     "algorithmic_bytes_per_launch": algorithmic},
+        "e2e": {"value": None, "unit": UNIT,
+                "reason": "inputs exceed host memory; drawn on the device, no host copies",
+                "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "gpu_launches": launches,
         "clocks": sampler.summary(),
     }
     if cpu is not None:

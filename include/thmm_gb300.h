@@ -51,6 +51,11 @@ enum {
   THMM_RESERVE_MAXIMUM = 1u,
   THMM_RESERVE_SAMPLING = 2u,
   THMM_RESERVE_MARGINALS = 4u,
+  /* Extension: inputs and results stay on the device. No pinned host staging
+   * is allocated; Inputs/CategoricalInputs/Uniforms and the prepared calls
+   * raise THMM_LOGIC_ERROR. Write inputs through thmm_device_buffers_get,
+   * then thmm_device_inputs_ready and thmm_enqueue. */
+  THMM_RESERVE_DEVICE_ONLY = 8u,
   /* Extension: run the sum-product paths (partition, log partition,
    * marginals) in FP64 instead of the default FP32 with exact power-of-two
    * scaling. MAP and sampling always compute in the scalar width. */
@@ -334,6 +339,35 @@ thmm_status thmm_categorical_posterior_marginals(
  * processed. */
 thmm_status thmm_enqueue(thmm_workspace *workspace, int operation,
                          uint64_t *nodes_out);
+
+/* Extension (no reference counterpart): inputs and results on the device.
+ * Device addresses of the workspace's input and result buffers, in the
+ * layouts of the prepared calls ([item][node][K], [edge][K][K], observation
+ * bytes, ...); null where the workspace has no such buffer. They stay valid
+ * until the workspace is reserved again or destroyed. For inputs produced on
+ * the GPU (for example by another kernel, or too large to stage through the
+ * host): write them here, then call thmm_device_inputs_ready; results of
+ * thmm_enqueue can be read here without a host copy. */
+typedef struct {
+  void *node_potentials;     /* dense: [batch][node][K] */
+  void *edge_potentials;     /* [edge][K][K] */
+  uint8_t *observations;     /* categorical: observation bytes */
+  void *root_potential;      /* categorical: [K] */
+  void *emission_potentials; /* categorical: [category][K] */
+  void *uniforms;            /* sampling: [batch][node] */
+  void *values;              /* [item]: log Z, Z or MAP log weight */
+  void *node_marginals;      /* [batch][node][K] */
+  void *edge_marginals;      /* [batch][edge][K][K] */
+  uint32_t *states;          /* [batch][node] MAP states or samples */
+} thmm_device_buffers;
+thmm_status thmm_device_buffers_get(thmm_workspace *workspace, thmm_device_buffers *out);
+/* Declares the device inputs the caller wrote into thmm_device_buffers_get's
+ * buffers resident for `batch` items (a forest: all its trees), as a prepared
+ * call with kAll leaves them, so that thmm_enqueue runs on them, and rebuilds
+ * the data the kernels derive from them. Work is queued on the workspace
+ * stream: the caller's writes must be complete (or queued earlier on that
+ * stream) when this is called. */
+thmm_status thmm_device_inputs_ready(thmm_workspace *workspace, size_t batch);
 
 /* Launch tuning of a workspace (extension, no reference counterpart). Trees
  * with at least `team_threshold` nodes are contracted by a whole CTA, smaller

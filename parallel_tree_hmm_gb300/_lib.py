@@ -31,6 +31,7 @@ THMM_SCALAR_F64 = 8
 THMM_RESERVE_MAXIMUM = 1
 THMM_RESERVE_SAMPLING = 2
 THMM_RESERVE_MARGINALS = 4
+THMM_RESERVE_DEVICE_ONLY = 8
 THMM_COMPUTE_F64 = 0x100
 THMM_COMPUTE_BF16 = 0x200
 THMM_UPDATE_ALL = 0
@@ -113,6 +114,13 @@ class MarginalResult(ctypes.Structure):
                 ("timings", Timings)]
 
 
+class DeviceBuffers(ctypes.Structure):
+    _fields_ = [(name, c_void_p) for name in (
+        "node_potentials", "edge_potentials", "observations", "root_potential",
+        "emission_potentials", "uniforms", "values", "node_marginals", "edge_marginals",
+        "states")]
+
+
 class Tuning(ctypes.Structure):
     _fields_ = [("team_threshold", c_u32), ("ctas_per_sm", c_u32 * 4),
                 ("stripes", c_u32), ("kernel_ms", ctypes.c_float), ("candidates", c_u32),
@@ -179,6 +187,8 @@ PROTOTYPES = {
     "thmm_workspace_synchronize": (c_int, [c_void_p]),
     "thmm_workspace_launches": (c_u64, [c_void_p]),
     "thmm_wait_timeout_check": (c_int, [c_int, c_u64]),
+    "thmm_device_buffers_get": (c_int, [c_void_p, ctypes.POINTER(DeviceBuffers)]),
+    "thmm_device_inputs_ready": (c_int, [c_void_p, c_size]),
     "thmm_log_partition_static": (c_int, [c_void_p, c_size, c_size, c_void_p, c_void_p,
                                           c_void_p, c_void_p]),
 }

@@ -233,6 +233,9 @@ class Workspace:
         self._plans: list[Plan] = []
         self._observation_nodes = np.zeros(0, dtype=np.uint32)
         self._capacity = 0
+        self._forest = False
+        self._states = 0
+        self._categories = 0
 
     def __del__(self):
         handle = getattr(self, "_handle", None)
@@ -252,7 +255,8 @@ class Workspace:
     def _flags(kind: str, compute) -> int:
         table = {"": 0, "maximum": _lib.THMM_RESERVE_MAXIMUM,
                  "sampling": _lib.THMM_RESERVE_SAMPLING,
-                 "marginals": _lib.THMM_RESERVE_MARGINALS}
+                 "marginals": _lib.THMM_RESERVE_MARGINALS,
+                 "device": _lib.THMM_RESERVE_DEVICE_ONLY}
         flags = 0
         for part in kind.split(","):  # e.g. "maximum,sampling"
             flags |= table[part.strip()]
@@ -270,6 +274,7 @@ class Workspace:
 
     # ------------------------------------------------------------- reserve
     def _reserve(self, kind, plan, states, batch_capacity, device, scalar, compute):
+        self._forest, self._states = False, states
         self._plans = [plan]
         self._capacity = batch_capacity
         self._observation_nodes = np.zeros(0, dtype=np.uint32)
@@ -296,6 +301,7 @@ class Workspace:
     def _reserve_categorical(self, kind, plan, states, batch_capacity, categories,
                              observation_nodes, device, scalar, compute):
         nodes = np.ascontiguousarray(observation_nodes, dtype=np.uint32)
+        self._forest, self._states, self._categories = False, states, categories
         self._plans = [plan]
         self._capacity = batch_capacity
         self._observation_nodes = nodes
@@ -331,6 +337,7 @@ class Workspace:
     def reserve_forest(self, plans, states, device=0, *, kind="", scalar=np.float64,
                        compute=None):
         """Extension: one independent tree per plan, each with its own edges."""
+        self._forest, self._states = True, states
         self._plans = list(plans)
         self._capacity = len(self._plans)
         self._observation_nodes = np.zeros(0, dtype=np.uint32)
@@ -344,6 +351,7 @@ class Workspace:
                                    compute=None):
         """Extension: categorical forest; `observation_nodes[t]` lists tree t's
         observed nodes (strictly increasing)."""
+        self._forest, self._states, self._categories = True, states, categories
         self._plans = list(plans)
         self._capacity = len(self._plans)
         counts = np.array([len(o) for o in observation_nodes], dtype=np.uint64)
@@ -384,6 +392,49 @@ class Workspace:
         _check(self._lib.thmm_uniforms(self._handle, self._batch(batch),
                                        ctypes.byref(address), ctypes.byref(count)))
         return _view(address.value, count.value, self._dtype)
+
+    def device_buffers(self) -> dict:
+        """Extension: zero-copy torch CUDA views of the workspace's device
+        input and result buffers (thmm_device_buffers_get), keyed by name;
+        absent where the workspace has no such buffer. Write inputs produced
+        on the GPU into them, then call device_inputs_ready(); read the
+        results of enqueue() from them. Valid until the next reserve."""
+        import torch
+
+        buffers = _lib.DeviceBuffers()
+        _check(self._lib.thmm_device_buffers_get(self._handle, ctypes.byref(buffers)))
+        K = self._states
+        if self._forest:
+            nodes = sum(p.num_nodes for p in self._plans)
+            edges_in = edges_out = sum(p.num_edges for p in self._plans)
+        else:
+            nodes = self._capacity * self._plans[0].num_nodes
+            edges_in = self._plans[0].num_edges
+            edges_out = self._capacity * edges_in
+        scalar = "<f8" if self._dtype == np.float64 else "<f4"
+        shapes = {"node_potentials": (nodes * K, scalar),
+                  "edge_potentials": (edges_in * K * K, scalar),
+                  "observations": (len(self._observation_nodes) *
+                                   (1 if self._forest else self._capacity), "|u1"),
+                  "root_potential": (K, scalar),
+                  "emission_potentials": (None, scalar),
+                  "uniforms": (nodes, scalar), "values": (self._capacity, scalar),
+                  "node_marginals": (nodes * K, scalar),
+                  "edge_marginals": (edges_out * K * K, scalar), "states": (nodes, "<u4")}
+        out = {}
+        for name, (count, typestr) in shapes.items():
+            address = getattr(buffers, name)
+            if not address:
+                continue
+            if count is None:  # emission table: categories x K
+                count = self._categories * K
+            out[name] = torch.as_tensor(_DeviceArray(address, count, typestr), device="cuda")
+        return out
+
+    def device_inputs_ready(self, batch=None) -> None:
+        """Extension: the device inputs written through device_buffers() are
+        resident for `batch` items (thmm_device_inputs_ready)."""
+        _check(self._lib.thmm_device_inputs_ready(self._handle, self._batch(batch)))
 
     def _plan_or_none(self):
         return self._plans[0] if len(self._plans) == 1 else None
@@ -544,6 +595,16 @@ class Workspace:
     @property
     def launches(self) -> int:
         return self._lib.thmm_workspace_launches(self._handle)
+
+
+class _DeviceArray:
+    """A device buffer described by the CUDA array interface (for
+    torch.as_tensor without a copy)."""
+
+    def __init__(self, address: int, count: int, typestr: str):
+        self.__cuda_array_interface__ = {"shape": (count,), "typestr": typestr,
+                                         "data": (address, False), "version": 3,
+                                         "strides": None}
 
 
 def _tuning_dict(tuning) -> dict:

@@ -131,6 +131,7 @@ struct Workspace {
   int scalar = THMM_SCALAR_F64;
   bool compute_f64 = false;
   bool bf16 = false; // BF16 tier of the tensor-core engine
+  bool device_only = false; // no host staging (THMM_RESERVE_DEVICE_ONLY)
   bool maximum = false;
   bool sampling = false;
   bool marginals = false;
@@ -366,6 +367,7 @@ struct Workspace {
     scalar = static_cast<int>(scalar_bytes);
     compute_f64 = (flags & THMM_COMPUTE_F64) != 0;
     bf16 = (flags & THMM_COMPUTE_BF16) != 0;
+    device_only = (flags & THMM_RESERVE_DEVICE_ONLY) != 0;
     maximum = (flags & THMM_RESERVE_MAXIMUM) != 0;
     sampling = (flags & THMM_RESERVE_SAMPLING) != 0;
     marginals = (flags & THMM_RESERVE_MARGINALS) != 0;
@@ -517,35 +519,41 @@ struct Workspace {
     // Inputs, outputs and scratch.
     const std::size_t S = ScalarBytes();
     const std::uint64_t edge_values = edge_inputs * KK;
+    // Pinned host staging, unless the workspace is reserved for device
+    // inputs only (THMM_RESERVE_DEVICE_ONLY).
+    const auto host = [&](HostBuffer &buffer, std::size_t size) {
+      if (!device_only)
+        buffer.Allocate(size);
+    };
     if (!categorical) {
       node_in.Allocate(total_nodes * K * S);
-      h_node_in.Allocate(total_nodes * K * S);
+      host(h_node_in, total_nodes * K * S);
     } else {
       observations.Allocate(total_observations);
-      h_observations.Allocate(total_observations);
+      host(h_observations, total_observations);
       root_potential.Allocate(K * S);
-      h_root.Allocate(K * S);
+      host(h_root, K * S);
       emission.Allocate(categories * K * S);
-      h_emission.Allocate(categories * K * S);
+      host(h_emission, categories * K * S);
     }
     edge_in.Allocate(edge_values * S);
-    h_edge_in.Allocate(edge_values * S);
+    host(h_edge_in, edge_values * S);
     values.Allocate(count * S);
-    h_values.Allocate(count * S);
+    host(h_values, count * S);
     h_control.Allocate(16);
     if (marginals) {
       node_out.Allocate(total_nodes * K * S);
-      h_node_out.Allocate(total_nodes * K * S);
+      host(h_node_out, total_nodes * K * S);
       edge_out.Allocate(total_edges_out * KK * S);
-      h_edge_out.Allocate(total_edges_out * KK * S);
+      host(h_edge_out, total_edges_out * KK * S);
     }
     if (maximum || sampling) {
       states_out.Allocate(total_nodes * sizeof(std::uint32_t));
-      h_states.Allocate(total_nodes * sizeof(std::uint32_t));
+      host(h_states, total_nodes * sizeof(std::uint32_t));
     }
     if (sampling) {
       uniforms.Allocate(total_nodes * S);
-      h_uniforms.Allocate(total_nodes * S);
+      host(h_uniforms, total_nodes * S);
     }
     scratch.Allocate(scratch_base * compute_bytes);
     bytes.Allocate(byte_base);
@@ -654,6 +662,12 @@ struct Workspace {
   void RequireReserved() const {
     if (!reserved)
       throw std::logic_error("accelerator Workspace::Reserve must precede Inputs");
+  }
+  void RequireStaging() const {
+    if (device_only)
+      throw std::logic_error(
+          "workspace reserved for device inputs only has no host staging: write the inputs "
+          "through thmm_device_buffers_get and run thmm_enqueue");
   }
 
   std::size_t NodesFor(std::size_t batch) const {
@@ -1098,6 +1112,7 @@ struct Workspace {
 
   Outcome Run(int operation, std::size_t batch, const std::vector<Upload> &uploads,
               Clock::time_point wall_start) {
+    RequireStaging();
     Check(cudaSetDevice(device), "cudaSetDevice");
     for (const Upload &upload : uploads)
       if (upload.source != upload.staging->ptr && upload.bytes != 0)
@@ -1713,6 +1728,7 @@ thmm_status thmm_inputs(thmm_workspace *workspace, size_t batch,
   return Guard([&] {
     Workspace &ws = thmm::AsWorkspace(workspace);
     ws.RequireReserved();
+    ws.RequireStaging();
     if (ws.categorical)
       throw std::logic_error(
           "accelerator dense Inputs cannot be used after ReserveCategorical");
@@ -1733,6 +1749,7 @@ thmm_status thmm_categorical_inputs(thmm_workspace *workspace, size_t batch,
     if (!ws.reserved || !ws.categorical)
       throw std::logic_error("accelerator Workspace::ReserveCategorical must "
                              "precede CategoricalInputs");
+    ws.RequireStaging();
     ws.CheckBatch(batch, "categorical input");
     *out = {ws.states,
             batch,
@@ -1757,6 +1774,7 @@ thmm_status thmm_uniforms(thmm_workspace *workspace, size_t batch, void **out,
     if (!ws.reserved || !ws.sampling)
       throw std::logic_error(
           "accelerator Workspace::ReserveSampling must precede Uniforms");
+    ws.RequireStaging();
     ws.CheckBatch(batch, "uniform");
     *out = ws.h_uniforms.ptr;
     *count = ws.NodesFor(batch);
@@ -1964,6 +1982,41 @@ thmm_status thmm_enqueue(thmm_workspace *workspace, int operation,
     ws.EnqueueGraph(operation, ws.last_batch);
     if (nodes_out != nullptr)
       *nodes_out = ws.NodesFor(ws.last_batch);
+  });
+}
+
+thmm_status thmm_device_buffers_get(thmm_workspace *workspace, thmm_device_buffers *out) {
+  return Guard([&] {
+    Workspace &ws = thmm::AsWorkspace(workspace);
+    if (out == nullptr)
+      throw std::invalid_argument("output must not be null");
+    ws.RequireReserved();
+    *out = thmm_device_buffers{};
+    out->node_potentials = ws.node_in.ptr;
+    out->edge_potentials = ws.edge_in.ptr;
+    out->observations = ws.observations.as<std::uint8_t>();
+    out->root_potential = ws.root_potential.ptr;
+    out->emission_potentials = ws.emission.ptr;
+    out->uniforms = ws.uniforms.ptr;
+    out->values = ws.values.ptr;
+    out->node_marginals = ws.node_out.ptr;
+    out->edge_marginals = ws.edge_out.ptr;
+    out->states = ws.states_out.as<std::uint32_t>();
+  });
+}
+
+thmm_status thmm_device_inputs_ready(thmm_workspace *workspace, size_t batch) {
+  return Guard([&] {
+    Workspace &ws = thmm::AsWorkspace(workspace);
+    ws.RequireReserved();
+    ws.CheckBatch(batch, "device input");
+    thmm::Check(cudaSetDevice(ws.device), "cudaSetDevice");
+    if (ws.categorical)
+      ws.OrderObservations(ws.stream);
+    ws.resident_observation_batch = batch;
+    ws.resident_factors = true;
+    ws.last_batch = batch;
+    ws.has_run = true;
   });
 }
 

@@ -141,10 +141,12 @@ def test_wide_batch_and_categorical_api(gpu):
 
 # BF16 tier (THMM_COMPUTE_BF16): one BF16 pass per product, about 8
 # significant bits per operand instead of FP32's 24. Its own, looser bars,
-# about three times the worst errors measured on a GB300 for these shapes;
-# it does not meet the 1e-6 / 1e-5 bars, which the default 3xTF32 tier meets.
-BF16_LOG_Z_RTOL = 2e-3
-BF16_MARGINAL_ATOL = 2e-2
+# about three to five times the worst errors measured on a GB300 for these
+# shapes (log Z 5.8e-6 at K = 64 and 7.1e-6 at 128; node marginals 2.1e-3
+# and 1.8e-3; edge marginals 3.0e-3 and 1.6e-3). It does not meet the
+# 1e-6 / 1e-5 bars, which the default 3xTF32 tier meets.
+BF16_LOG_Z_RTOL = 3e-5
+BF16_MARGINAL_ATOL = 1e-2
 
 
 @pytest.mark.parametrize("K", [64, 128])
