@@ -73,6 +73,9 @@ def parse_args():
                              "many windows, inputs drawn on the GPU (full-size runs)")
     parser.add_argument("--precision", choices=["tf32x3", "bf16"], default="tf32x3",
                         help="dense workload above 32 states: tensor-core product tier")
+    parser.add_argument("--schedule", choices=["phases", "teams"], default="phases",
+                        help="dense workload above 32 states: every round of every tree "
+                             "grid-wide (phases) or one CTA per tree (teams)")
     parser.add_argument("--check-trees", type=int, default=16,
                         help="gw workload: trees checked against the oracle")
     parser.add_argument("--workload", choices=["forest", "gw", "dense"], default="forest",
@@ -915,6 +918,7 @@ def run_dense(args, rank, world, local_rank, dist):
     ws = thmm.Workspace()
     ws.reserve_forest(plans, K, device, kind="marginals", scalar=np.float32,
                       compute="bf16" if args.precision == "bf16" else None)
+    select_schedule(ws, args)
     staged = ws.inputs()
     staged.node_potentials[:] = node_factors
 
@@ -953,6 +957,7 @@ def run_dense(args, rank, world, local_rank, dist):
             ws.enqueue(4)
         end.record(ext)
         end.synchronize()
+    launches = ws.launches
     step_ms = reduce_max(begin.elapsed_time(end), dist) / args.steps
     value = total_nodes * world / (step_ms / 1e3)
 
@@ -968,8 +973,8 @@ def run_dense(args, rank, world, local_rank, dist):
     S = 4
     algorithmic = (2 * total_edges * K * K * S + 2 * total_nodes * K * S + len(plans) * S)
     # Useful tensor-core work: 2 K^3 per product, one product per compression
-    # forward and three in the adjoint.
-    useful_flops = 4 * 2 * compressions * K ** 3
+    # forward and two in the adjoint.
+    useful_flops = 3 * 2 * compressions * K ** 3
     peaks = json.loads((ROOT / "MEASURED_PEAKS.json").read_text()) \
         if (ROOT / "MEASURED_PEAKS.json").exists() else {}
     peak = peaks.get("hbm_gbs", 6800.0)
@@ -982,6 +987,7 @@ def run_dense(args, rank, world, local_rank, dist):
                   if args.precision == "bf16" else "f32 (3xTF32 tensor-core products)"),
         "data": "synthetic",
         "config": {**config, "all_log_z_finite": finite, "precision_tier": args.precision,
+                   "schedule": args.schedule if K > 32 else None,
                    "accuracy_vs_fp64_oracle": accuracy,
                    "node_marginal_normalisation_error": node_sum_error,
                    ("useful_tensor_tflops" if K > 32 else "useful_product_tflops"):
@@ -994,13 +1000,24 @@ def run_dense(args, rank, world, local_rank, dist):
                 "h2d_bytes_per_step": (total_edges * K * K + total_nodes * K) * S,
                 "d2h_bytes_per_step": (total_edges * K * K + total_nodes * K) * S
                 + len(plans) * S + 16},
-        "gpu_launches": 2 * args.steps,
+        "gpu_launches": launches * args.steps,
         "clocks": sampler.summary(),
     }
     if cpu is not None:
         line["cpu_baseline"] = cpu
     if rank == 0:
         print(json.dumps(line), flush=True)
+
+
+def select_schedule(ws, args):
+    """Applies --schedule to a workspace above 32 states (the forest default
+    is the phase schedule)."""
+    from parallel_tree_hmm_gb300 import _lib
+
+    if args.states > 32:
+        wanted = (_lib.THMM_SCHEDULE_PHASES if args.schedule == "phases"
+                  else _lib.THMM_SCHEDULE_TEAMS)
+        ws.set_tuning(ws.tuning["team_threshold"], schedule=wanted)
 
 
 def run_dense_streamed(args, rank, world, local_rank, dist, parents):
@@ -1043,6 +1060,7 @@ def run_dense_streamed(args, rank, world, local_rank, dist, parents):
             plans = thmm.Plan.many(parents[bounds[w]:bounds[w + 1]])
             ws.reserve_forest(plans, K, device, kind="marginals,device", scalar=np.float32,
                               compute="bf16" if args.precision == "bf16" else None)
+            select_schedule(ws, args)
             buffers = ws.device_buffers()
             fill(buffers["node_potentials"], 1.0, 0.0)
             fill(buffers["edge_potentials"], args.edge_sigma, args.zero_fraction)
@@ -1111,7 +1129,8 @@ def run_dense_streamed(args, rank, world, local_rank, dist, parents):
                    "all_log_z_finite": finite,
                    "node_marginal_normalisation_error": node_sum_error,
                    ("useful_tensor_tflops" if K > 32 else "useful_product_tflops"):
-                       4 * 2 * compressions * K ** 3 / (total_ms / 1e3) / 1e12,
+                       3 * 2 * compressions * K ** 3 / (total_ms / 1e3) / 1e12,
+                   "schedule": args.schedule if K > 32 else None,
                    "l2": "inputs larger than L2"},
         "roofline": {"bound": "hbm", "achieved": algorithmic / (total_ms / 1e3) / 1e9,
                      "peak": peak, "unit": "GB/s",

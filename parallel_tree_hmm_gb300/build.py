@@ -54,6 +54,7 @@ SOURCES = [
     "engine_sample_f32.cu",
     "engine_wide.cu",
     "engine_phase.cu",
+    "engine_wide_phase.cu",
     "engine_linear_f32.cu",
     "engine_linear_f64.cu",
     "engine_maximum.cu",

@@ -92,6 +92,10 @@ cudaError_t LaunchObservationGather(const std::uint8_t *observations,
 
 cudaError_t LaunchPhase(int scalar_bytes, bool compute_f64, int kind, const PhaseArgs &args,
                         cudaStream_t stream, int *blocks_per_sm) {
+  if (args.states > 32)
+    return scalar_bytes == 4 && !compute_f64 && !args.batch
+               ? LaunchWidePhase(kind, args, stream, blocks_per_sm)
+               : cudaErrorInvalidValue;
   if (scalar_bytes == 8)
     return compute_f64 ? LaunchTyped<double, double>(kind, args, stream, blocks_per_sm)
                        : LaunchTyped<double, float>(kind, args, stream, blocks_per_sm);

@@ -1,4 +1,5 @@
-// Level-synchronous phase schedule for small state counts (K <= 4).
+// Level-synchronous phase schedule for small (K <= 4) and wide
+// (32 < K <= 128) state counts.
 //
 // The per-tree engine (engine.cuh) contracts one tree per team and walks the
 // tree's plan step by step with a team barrier in between; a tree has 20-50
@@ -109,6 +110,10 @@ struct PhaseArgs {
   std::uint64_t item_stride;
   std::uint64_t item_nodes;
   std::uint64_t item_edges;
+  // Wide-state kinds (32 < K <= 128) only: the error word (tensor-core wait
+  // time-outs) and the BF16 product tier.
+  std::uint32_t *error;
+  std::uint32_t bf16;
 };
 
 // Operation counts of one program per round and kind.
@@ -168,9 +173,13 @@ PhasePlan BuildPhasePlan(const ProgramSet &set, std::span<const PhaseInstance> i
 
 // Launches one phase (or reports its occupancy when blocks_per_sm is
 // non-null). scalar_bytes: 4 or 8 (input/output type); compute_f64: FP64
-// arithmetic. Only padded state count 4 (K <= 4) has a phase schedule.
+// arithmetic. Padded state count 4 (K <= 4) runs one thread per operation
+// (phase_engine.cuh); 32 < K <= 128 (FP32 only, forest layout, no tail
+// kinds) one CTA per operation (wide_phase.cuh).
 cudaError_t LaunchPhase(int scalar_bytes, bool compute_f64, int kind, const PhaseArgs &args,
                         cudaStream_t stream, int *blocks_per_sm);
+cudaError_t LaunchWidePhase(int kind, const PhaseArgs &args, cudaStream_t stream,
+                            int *blocks_per_sm);
 
 // The phase-ordered copy of the observations: ordered[j * items + b] =
 // observations[b * per_item + order[j]] for j < count, b < items (a forest:

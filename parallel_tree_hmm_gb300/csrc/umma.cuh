@@ -156,6 +156,12 @@ __device__ __forceinline__ void BulkLoad(void *dst, const void *src, std::uint32
                "l"(src), "r"(bytes), "r"(SmemAddress(barrier))
                : "memory");
 }
+// Starts fetching `bytes` of global memory into L2 (a hint: nothing waits
+// on it). Address and size are multiples of 16 bytes.
+__device__ __forceinline__ void PrefetchL2(const void *src, std::uint32_t bytes) {
+  asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(src), "r"(bytes) : "memory");
+}
+
 // Orders this thread's earlier generic-proxy memory accesses before later
 // async-proxy (TMA, tensor core) accesses of the same memory, and back.
 __device__ __forceinline__ void FenceProxy() {

@@ -1,7 +1,11 @@
 """Wide state counts (32 < K <= 128): the tensor-core sum-product engine.
 
 Compress products and their adjoints run on tcgen05 in 3xTF32 with FP32
-accumulation; everything else is FP32 with exact power-of-two scaling.
+accumulation; everything else is FP32 with exact power-of-two scaling. A
+forest runs on the phase schedule by default (every round of every tree in
+grid-wide launches, wide_phase.cuh); the per-tree schedule (one CTA per
+tree, wide_engine.cuh) is selected with set_tuning(schedule=TEAMS), and
+every forest test runs on both.
 Tolerances against the FP64 oracle:
   * log Z: relative error <= 1e-6 for every K (the narrow FP32 engine's bar).
     The forward compress products keep their hi*hi parts per depth chunk and
@@ -16,7 +20,7 @@ import numpy as np
 import pytest
 
 from oracle import bridge
-from parallel_tree_hmm_gb300 import synthetic
+from parallel_tree_hmm_gb300 import _lib, synthetic
 
 pytestmark = pytest.mark.gpu
 
@@ -39,11 +43,19 @@ def shapes(rng, scale):
     }
 
 
-def check_forest(gpu, plans, K, nodes, edges, compute=None, tolerances=None):
+SCHEDULES = ["phases", "teams"]
+
+
+def check_forest(gpu, plans, K, nodes, edges, compute=None, tolerances=None,
+                 schedule="phases"):
     """Forest marginals against the FP64 oracle; returns the worst log Z
     relative, node and edge absolute errors."""
     ws = gpu.Workspace()
     ws.reserve_forest(plans, K, kind="marginals", scalar=np.float32, compute=compute)
+    wanted = _lib.THMM_SCHEDULE_PHASES if schedule == "phases" else _lib.THMM_SCHEDULE_TEAMS
+    assert ws.tuning["schedule"] == _lib.THMM_SCHEDULE_PHASES  # the forest default
+    ws.set_tuning(ws.tuning["team_threshold"], schedule=wanted)
+    assert ws.tuning["schedule"] == wanted
     view = ws.posterior_marginals_prepared(
         gpu.BatchedModelView(None, K, len(plans), nodes, edges))
     log_z = np.array(view.log_partitions, dtype=np.float64)
@@ -75,8 +87,8 @@ def check_forest(gpu, plans, K, nodes, edges, compute=None, tolerances=None):
         worst[1] = max(worst[1], np.max(np.abs(got_nodes[n0 * K:n1 * K] - node_m)))
         worst[2] = max(worst[2], np.max(np.abs(got_edges[e0 * K * K:e1 * K * K] - edge_m),
                                         initial=0.0))
-    print(f"K={K} {compute or 'tf32x3'}: log Z rel {worst[0]:.2e}, node {worst[1]:.2e}, "
-          f"edge {worst[2]:.2e}")
+    print(f"K={K} {compute or 'tf32x3'} {schedule}: log Z rel {worst[0]:.2e}, "
+          f"node {worst[1]:.2e}, edge {worst[2]:.2e}")
     log_z_tol, marginal_tol = tolerances or (log_z_rtol(K), MARGINAL_ATOL)
     assert worst[0] <= log_z_tol
     assert worst[1] <= marginal_tol
@@ -84,8 +96,9 @@ def check_forest(gpu, plans, K, nodes, edges, compute=None, tolerances=None):
     return worst
 
 
+@pytest.mark.parametrize("schedule", SCHEDULES)
 @pytest.mark.parametrize("K", [33, 64, 100, 128])
-def test_wide_marginals_against_fp64_oracle(gpu, K):
+def test_wide_marginals_against_fp64_oracle(gpu, K, schedule):
     rng = np.random.default_rng(900 + K)
     scale = 100 if K <= 64 else 40
     plans = [gpu.Plan(p) for p in shapes(rng, scale).values()]
@@ -93,10 +106,11 @@ def test_wide_marginals_against_fp64_oracle(gpu, K):
     edge_total = sum(p.num_edges for p in plans)
     nodes = (rng.random(node_total * K) * 0.9 + 0.1).astype(np.float32)
     edges = synthetic.stochastic_edges(rng, edge_total, K, 0.5).astype(np.float32)
-    check_forest(gpu, plans, K, nodes, edges)
+    check_forest(gpu, plans, K, nodes, edges, schedule=schedule)
 
 
-def test_wide_lognormal_factors_with_zeros(gpu):
+@pytest.mark.parametrize("schedule", SCHEDULES)
+def test_wide_lognormal_factors_with_zeros(gpu, schedule):
     """Dense-contraction workload shapes: spine-heavy trees, K = 64, edge
     factors lognormal(0, 2) with 5% exact zeros."""
     rng = np.random.default_rng(64)
@@ -107,6 +121,24 @@ def test_wide_lognormal_factors_with_zeros(gpu):
     nodes = synthetic.lognormal(rng, node_total * K, 1.0).astype(np.float32)
     edges = synthetic.lognormal(rng, edge_total * K * K, 2.0,
                                 zero_fraction=0.05).astype(np.float32)
+    check_forest(gpu, plans, K, nodes, edges, schedule=schedule)
+
+
+@pytest.mark.parametrize("K", [40, 64, 128])
+def test_wide_phases_many_trees(gpu, K):
+    """More operations per round than CTAs in the persistent grid (each CTA
+    takes several), trees of very different depth in one launch sequence, a
+    categorical-free dense forest with zeros."""
+    rng = np.random.default_rng(3100 + K)
+    sizes = rng.integers(2, 160 if K < 128 else 60, size=300)
+    parents = [synthetic.spine_heavy(rng, int(n)) if t % 2 else
+               synthetic.random_recursive(rng, int(n)) for t, n in enumerate(sizes)]
+    plans = [gpu.Plan(p) for p in parents]
+    node_total = sum(p.num_nodes for p in plans)
+    edge_total = sum(p.num_edges for p in plans)
+    nodes = synthetic.lognormal(rng, node_total * K, 1.0).astype(np.float32)
+    edges = synthetic.lognormal(rng, edge_total * K * K, 1.0,
+                                zero_fraction=0.02).astype(np.float32)
     check_forest(gpu, plans, K, nodes, edges)
 
 
@@ -149,8 +181,9 @@ BF16_LOG_Z_RTOL = 3e-5
 BF16_MARGINAL_ATOL = 1e-2
 
 
+@pytest.mark.parametrize("schedule", SCHEDULES)
 @pytest.mark.parametrize("K", [64, 128])
-def test_wide_bf16_tier_against_fp64_oracle(gpu, K, capsys):
+def test_wide_bf16_tier_against_fp64_oracle(gpu, K, schedule, capsys):
     rng = np.random.default_rng(1600 + K)
     plans = [gpu.Plan(synthetic.spine_heavy(rng, n)) for n in (150, 300)]
     plans += [gpu.Plan(np.arange(-1, 40))]
@@ -161,7 +194,7 @@ def test_wide_bf16_tier_against_fp64_oracle(gpu, K, capsys):
                                 zero_fraction=0.05).astype(np.float32)
     with capsys.disabled():
         check_forest(gpu, plans, K, nodes, edges, compute="bf16",
-                     tolerances=(BF16_LOG_Z_RTOL, BF16_MARGINAL_ATOL))
+                     tolerances=(BF16_LOG_Z_RTOL, BF16_MARGINAL_ATOL), schedule=schedule)
 
 
 def test_wide_limits(gpu):
