@@ -12,6 +12,11 @@ cudaError_t LaunchWideKind(const PhaseArgs &args, cudaStream_t stream, int *bloc
   const int smem = static_cast<int>(kTensor ? L::kSmemBytes : wide::kVectorBytes);
   cudaError_t status =
       cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+  // The largest shared-memory carve-out, so that the occupancy query (and
+  // the SM) count on as many resident CTAs as the layout allows.
+  if (status == cudaSuccess && kTensor)
+    status = cudaFuncSetAttribute(kernel, cudaFuncAttributePreferredSharedMemoryCarveout,
+                                  cudaSharedmemCarveoutMaxShared);
   if (status != cudaSuccess)
     return status;
   int per_sm = 0;
@@ -24,7 +29,7 @@ cudaError_t LaunchWideKind(const PhaseArgs &args, cudaStream_t stream, int *bloc
   if (args.count == 0)
     return cudaSuccess;
   if (kTensor)
-    per_sm = per_sm < L::kCtasPerSm ? per_sm : L::kCtasPerSm;
+    per_sm = L::kResident;
   int device = 0, sms = 0;
   status = cudaGetDevice(&device);
   if (status == cudaSuccess)

@@ -59,6 +59,13 @@ template <int KP> struct PhaseLayout {
   static constexpr unsigned kFloorBytes = 228 * 1024 / (kCtasPerSm + 1);
   static constexpr unsigned kSmemBytes = kUsedBytes > kFloorBytes ? kUsedBytes : kFloorBytes;
   static_assert(kSmemBytes <= 227 * 1024, "shared memory per CTA");
+  // CTAs per SM the grid is sized for: what the shared memory (with 1 KB of
+  // static and 1 KB of reserved shared memory per CTA) and TMEM allow. The
+  // occupancy query reports one CTA per SM for kernels that use tcgen05,
+  // whatever their resources, so it is not consulted.
+  static constexpr unsigned kSmemResident = 228 * 1024 / (kSmemBytes + 2048);
+  static constexpr int kResident =
+      static_cast<int>(kSmemResident) < kCtasPerSm ? static_cast<int>(kSmemResident) : kCtasPerSm;
 };
 
 // Dynamic shared memory of the kinds without tensor-core work: the vectors.
@@ -120,35 +127,47 @@ struct Columns {
 
 // The adjoint ratio of a compression, formed while staging: entry (r, c)
 // is mu[r][c] / product[r][c] with product = stored path * 2^shift (zero
-// where the product is zero), i.e. ScalePow2(mu / stored, -shift).
-__device__ __forceinline__ float RatioOf(float mu, float stored, int shift) {
-  return stored > 0.0f ? ScalePow2(mu / stored, -shift) : 0.0f;
-}
+// where the product is zero). The division is the fast reciprocal form
+// (stored entries are at most 1, well inside its range; about 2 ulp), and
+// 2^-shift is one exact factor when it is a normal float.
+struct Ratio {
+  int shift;
+  float factor;
+  bool exact;
+  __device__ __forceinline__ explicit Ratio(int s)
+      : shift(s), factor(s >= -127 && s <= 126 ? ScalePow2(1.0f, -s) : 0.0f),
+        exact(s >= -127 && s <= 126) {}
+  __device__ __forceinline__ float operator()(float mu, float stored) const {
+    if (!(stored > 0.0f))
+      return 0.0f;
+    const float q = __fdividef(mu, stored);
+    return exact ? q * factor : ScalePow2(q, -shift);
+  }
+};
 struct RatioRows {
   static constexpr bool kColumns = false;
   const float *mu;
   const float *stored;
-  int shift;
+  Ratio ratio;
   __device__ __forceinline__ float At(unsigned K, unsigned r, unsigned d) const {
     const std::size_t at = static_cast<std::size_t>(r) * K + d;
-    return RatioOf(mu[at], stored[at], shift);
+    return ratio(mu[at], stored[at]);
   }
   __device__ __forceinline__ float4 Quad(unsigned K, unsigned r, unsigned d) const {
     const std::size_t at = static_cast<std::size_t>(r) * K + d;
     const float4 m = *reinterpret_cast<const float4 *>(mu + at);
     const float4 s = *reinterpret_cast<const float4 *>(stored + at);
-    return make_float4(RatioOf(m.x, s.x, shift), RatioOf(m.y, s.y, shift),
-                       RatioOf(m.z, s.z, shift), RatioOf(m.w, s.w, shift));
+    return make_float4(ratio(m.x, s.x), ratio(m.y, s.y), ratio(m.z, s.z), ratio(m.w, s.w));
   }
 };
 struct RatioColumns {
   static constexpr bool kColumns = true;
   const float *mu;
   const float *stored;
-  int shift;
+  Ratio ratio;
   __device__ __forceinline__ float At(unsigned K, unsigned r, unsigned d) const {
     const std::size_t at = static_cast<std::size_t>(d) * K + r;
-    return RatioOf(mu[at], stored[at], shift);
+    return ratio(mu[at], stored[at]);
   }
 };
 
@@ -428,6 +447,20 @@ template <int KP> struct WideOps {
     return 0;
   }
 
+  // Row stride (floats) of a K x K tile staged in the operand buffers: K + 4,
+  // so that the 16-byte row writes of eight consecutive rows (one per
+  // thread) and the row reads of the coalesced passes are conflict-free.
+  __device__ __forceinline__ unsigned TileStride() const { return K + 4; }
+  // Writes columns [c, c + 32) ∩ [0, K) of row j of a tile (K % 4 == 0).
+  __device__ __forceinline__ void TileRow(float *tile, unsigned j, unsigned c,
+                                          const float (&row)[32]) const {
+#pragma unroll
+    for (unsigned q = 0; q < 32; q += 4)
+      if (c + q < K)
+        *reinterpret_cast<float4 *>(tile + j * TileStride() + c + q) =
+            make_float4(row[q], row[q + 1], row[q + 2], row[q + 3]);
+  }
+
   // Rows per warp whose loads are in flight together (MatVec, RakeReverse).
   static constexpr unsigned kRows = KP == 64 ? 8 : 4;
 
@@ -549,24 +582,39 @@ template <int KP> struct WideOps {
           m = m < row[q] ? row[q] : m;
     }
     const int s = ExponentOf(CtaMax(m, sh));
-    float *out = Comps() + static_cast<std::size_t>(i) * KK + static_cast<std::size_t>(j) * K;
+    float *out = Comps() + static_cast<std::size_t>(i) * KK;
+    if (K % 4 == 0) {
+      // Rows through the (now idle) operand buffers, then coalesced stores.
+      float *tile = reinterpret_cast<float *>(smem);
 #pragma unroll 1
-    for (unsigned c = 0; c < KP; c += 32) {
-      float row[32];
-      SplitSum32<KP>(lane_base, c, row, a.bf16 != 0);
-      if (j < K) {
-        if (K % 4 == 0) {
+      for (unsigned c = 0; c < KP; c += 32) {
+        float row[32];
+        SplitSum32<KP>(lane_base, c, row, a.bf16 != 0);
+        if (j < K) {
 #pragma unroll
-          for (unsigned q = 0; q < 32; q += 4)
-            if (c + q < K)
-              *reinterpret_cast<float4 *>(out + c + q) =
-                  make_float4(ScalePow2(row[q], -s), ScalePow2(row[q + 1], -s),
-                              ScalePow2(row[q + 2], -s), ScalePow2(row[q + 3], -s));
-        } else {
+          for (unsigned q = 0; q < 32; ++q)
+            row[q] = ScalePow2(row[q], -s);
+          TileRow(tile, j, c, row);
+        }
+      }
+      __syncthreads();
+      const unsigned quads = K / 4;
+#pragma unroll 4
+      for (unsigned f = threadIdx.x; f < K * quads; f += kThreads) {
+        const unsigned r = f / quads, c = 4 * (f % quads);
+        *reinterpret_cast<float4 *>(out + static_cast<std::size_t>(r) * K + c) =
+            *reinterpret_cast<const float4 *>(tile + r * TileStride() + c);
+      }
+    } else {
+#pragma unroll 1
+      for (unsigned c = 0; c < KP; c += 32) {
+        float row[32];
+        SplitSum32<KP>(lane_base, c, row, a.bf16 != 0);
+        if (j < K) {
 #pragma unroll
           for (unsigned q = 0; q < 32; ++q)
             if (c + q < K)
-              out[c + q] = ScalePow2(row[q], -s);
+              out[static_cast<std::size_t>(j) * K + c + q] = ScalePow2(row[q], -s);
         }
       }
     }
@@ -693,42 +741,101 @@ template <int KP> struct WideOps {
     const float *mu = CompMu() + static_cast<std::size_t>(i) * KK;
     const float *stored = Comps() + static_cast<std::size_t>(i) * KK;
     // P1[r][m] = sum_c R[r][c] right[m][c];  P2[m][c] = sum_r left[r][m] R[r][c].
-    ok = PhaseProduct<KP, false>(smem, sh, phase, tmem, K, RatioRows{mu, stored, shift},
+    const Ratio ratio_of(shift);
+    ok = PhaseProduct<KP, false>(smem, sh, phase, tmem, K, RatioRows{mu, stored, ratio_of},
                                  Rows{right, nullptr}, a.bf16 != 0) &&
          ok;
     ok = PhaseProduct<KP, false>(smem, sh, phase, tmem + KP, K, Columns{left},
-                                 RatioColumns{mu, stored, shift}, a.bf16 != 0) &&
+                                 RatioColumns{mu, stored, ratio_of}, a.bf16 != 0) &&
          ok;
     const std::uint32_t lane_base = tmem + ((threadIdx.x & ~31u) << 16);
-    float *left_out = AdjointOf(op.x) + static_cast<std::size_t>(j) * K;
-    float *right_out = AdjointOf(op.z) + static_cast<std::size_t>(j) * K;
-    const float *left_row = left + static_cast<std::size_t>(j) * K;
-    const float *right_row = right + static_cast<std::size_t>(j) * K;
-    const float middle_j = j < K ? middle[j] : 0.0f;
-    // (tcgen05.ld is warp-collective: every lane loads, lanes j >= K discard.)
-#pragma unroll 1
-    for (unsigned c = 0; c < KP; c += 32) {
-      float p1[32];
-      umma::Load32(lane_base + c, p1);
-      if (j < K) {
-#pragma unroll
-        for (unsigned q = 0; q < 32; ++q)
-          if (c + q < K)
-            left_out[c + q] = left_row[c + q] * middle[c + q] * p1[q];
-      }
-    }
+    float *left_out = AdjointOf(op.x);
+    float *right_out = AdjointOf(op.z);
     float total = 0.0f;
+    if (K % 4 == 0) {
+      // Each product's rows go through the (now idle) operand buffers; the
+      // adjoints are then formed and stored in coalesced passes.
+      float *tile = reinterpret_cast<float *>(smem);
+      const unsigned quads = K / 4;
+      const auto stage_rows = [&](std::uint32_t column) {
 #pragma unroll 1
-    for (unsigned c = 0; c < KP; c += 32) {
-      float p2[32];
-      umma::Load32(lane_base + KP + c, p2);
+        for (unsigned c = 0; c < KP; c += 32) {
+          float row[32];
+          umma::Load32(lane_base + column + c, row);
+          if (j < K)
+            TileRow(tile, j, c, row);
+        }
+        __syncthreads();
+      };
+      // Left adjoint left[r][m] middle[m] P1[r][m].
+      stage_rows(0);
+#pragma unroll 4
+      for (unsigned f = threadIdx.x; f < K * quads; f += kThreads) {
+        const unsigned r = f / quads, c = 4 * (f % quads);
+        const std::size_t at = static_cast<std::size_t>(r) * K + c;
+        const float4 l = *reinterpret_cast<const float4 *>(left + at);
+        const float4 p = *reinterpret_cast<const float4 *>(tile + r * TileStride() + c);
+        *reinterpret_cast<float4 *>(left_out + at) =
+            make_float4(l.x * middle[c] * p.x, l.y * middle[c + 1] * p.y,
+                        l.z * middle[c + 2] * p.z, l.w * middle[c + 3] * p.w);
+      }
+      __syncthreads();
+      // Right adjoint right[m][c] middle[m] P2[m][c], kept in the tile for
+      // the middle adjoint (its row sums).
+      stage_rows(KP);
+#pragma unroll 4
+      for (unsigned f = threadIdx.x; f < K * quads; f += kThreads) {
+        const unsigned r = f / quads, c = 4 * (f % quads);
+        const std::size_t at = static_cast<std::size_t>(r) * K + c;
+        const float4 rr = *reinterpret_cast<const float4 *>(right + at);
+        float4 *p = reinterpret_cast<float4 *>(tile + r * TileStride() + c);
+        const float mr = middle[r];
+        const float4 v = *p;
+        const float4 adjoint =
+            make_float4(rr.x * mr * v.x, rr.y * mr * v.y, rr.z * mr * v.z, rr.w * mr * v.w);
+        *reinterpret_cast<float4 *>(right_out + at) = adjoint;
+        *p = adjoint;
+      }
+      __syncthreads();
       if (j < K) {
+        const float *row = tile + j * TileStride();
+        for (unsigned c = 0; c < K; c += 4) {
+          const float4 v = *reinterpret_cast<const float4 *>(row + c);
+          total += v.x;
+          total += v.y;
+          total += v.z;
+          total += v.w;
+        }
+      }
+    } else {
+      // (tcgen05.ld is warp-collective: every lane loads, lanes j >= K discard.)
+      const float *left_row = left + static_cast<std::size_t>(j) * K;
+      const float *right_row = right + static_cast<std::size_t>(j) * K;
+      const float middle_j = j < K ? middle[j] : 0.0f;
+#pragma unroll 1
+      for (unsigned c = 0; c < KP; c += 32) {
+        float p1[32];
+        umma::Load32(lane_base + c, p1);
+        if (j < K) {
 #pragma unroll
-        for (unsigned q = 0; q < 32; ++q) {
-          if (c + q < K) {
-            const float adjoint = right_row[c + q] * middle_j * p2[q];
-            right_out[c + q] = adjoint;
-            total += adjoint;
+          for (unsigned q = 0; q < 32; ++q)
+            if (c + q < K)
+              left_out[static_cast<std::size_t>(j) * K + c + q] =
+                  left_row[c + q] * middle[c + q] * p1[q];
+        }
+      }
+#pragma unroll 1
+      for (unsigned c = 0; c < KP; c += 32) {
+        float p2[32];
+        umma::Load32(lane_base + KP + c, p2);
+        if (j < K) {
+#pragma unroll
+          for (unsigned q = 0; q < 32; ++q) {
+            if (c + q < K) {
+              const float adjoint = right_row[c + q] * middle_j * p2[q];
+              right_out[static_cast<std::size_t>(j) * K + c + q] = adjoint;
+              total += adjoint;
+            }
           }
         }
       }
