@@ -187,28 +187,54 @@ struct RatioColumns {
 //     depths, four coalesced 128-byte loads and one 16-byte store per thread.
 constexpr unsigned kBatch = 4;
 
-template <class Src> struct QuadSlots {
-  unsigned K, quads, quad_groups, total;
-  __device__ __forceinline__ QuadSlots(unsigned states, unsigned depth)
-      : K(states), quads(depth / 4), quad_groups((depth / 4 + 3) / 4),
-        total(Src::kColumns ? states * (depth / 4) : (states + 7) / 8 * ((depth / 4 + 3) / 4) * 32) {}
-  // Row and quad of slot idx; false for a padding slot.
-  __device__ __forceinline__ bool At(unsigned idx, unsigned &r, unsigned &q) const {
-    if (idx >= total)
-      return false;
+// This thread's walk over the quad slots of an operand chunk: slot
+// threadIdx.x, then every kThreads-th. The row and quad of each slot are
+// advanced incrementally (one division when the walk starts, none per slot).
+//   * Row sources: slot idx is lane t = idx % 32 of group g = idx / 32, row
+//     (g / quad_groups) * 8 + t % 8, quad (g % quad_groups) * 4 + t / 8;
+//   * column sources: row idx % K, quad idx / K.
+template <class Src> struct QuadCursor {
+  unsigned K, quads, quad_groups;
+  unsigned major, minor; // rows: g / quad_groups, g % quad_groups; columns: q, r
+  unsigned step_major, step_minor;
+  unsigned lane_row, lane_quad;
+  __device__ __forceinline__ QuadCursor(unsigned states, unsigned depth)
+      : K(states), quads(depth / 4), quad_groups((depth / 4 + 3) / 4) {
     if constexpr (Src::kColumns) {
-      r = idx % K;
-      q = idx / K;
-      return true;
+      major = threadIdx.x / K;
+      minor = threadIdx.x % K;
+      step_major = kThreads / K;
+      step_minor = kThreads % K;
+      lane_row = lane_quad = 0;
     } else {
-      const unsigned t = idx & 31u, g = idx >> 5;
-      r = (g / quad_groups) * 8 + (t & 7u);
-      q = (g % quad_groups) * 4 + (t >> 3);
-      return r < K && q < quads;
+      const unsigned g = threadIdx.x >> 5, t = threadIdx.x & 31u;
+      major = g / quad_groups;
+      minor = g % quad_groups;
+      step_major = (kThreads / 32) / quad_groups;
+      step_minor = (kThreads / 32) % quad_groups;
+      lane_row = t & 7u;
+      lane_quad = t >> 3;
     }
   }
-  __device__ __forceinline__ unsigned Passes() const {
-    return (total + kThreads * kBatch - 1) / (kThreads * kBatch);
+  __device__ __forceinline__ unsigned Row() const {
+    return Src::kColumns ? minor : major * 8 + lane_row;
+  }
+  __device__ __forceinline__ unsigned Quad() const {
+    return Src::kColumns ? major : minor * 4 + lane_quad;
+  }
+  // Slots remain (this one may still be padding).
+  __device__ __forceinline__ bool More() const {
+    return Src::kColumns ? major < quads : major * 8 < K;
+  }
+  __device__ __forceinline__ bool Valid() const { return More() && Row() < K && Quad() < quads; }
+  __device__ __forceinline__ void Advance() {
+    const unsigned limit = Src::kColumns ? K : quad_groups;
+    major += step_major;
+    minor += step_minor;
+    if (minor >= limit) {
+      minor -= limit;
+      ++major;
+    }
   }
 };
 
@@ -278,30 +304,88 @@ __device__ __forceinline__ void StageChunk(const XS &x, const YS &y, unsigned K,
     StageScalar<kBf16>(y, K, d0, depth, yh, yl);
     return;
   }
-  const QuadSlots<XS> xs(K, depth);
-  const QuadSlots<YS> ys(K, depth);
-  const unsigned passes = xs.Passes() > ys.Passes() ? xs.Passes() : ys.Passes();
+  QuadCursor<XS> xs(K, depth);
+  QuadCursor<YS> ys(K, depth);
 #pragma unroll 1
-  for (unsigned pass = 0; pass < passes; ++pass) {
+  while (xs.More() || ys.More()) {
     float4 xv[kBatch], yv[kBatch];
-    const unsigned base = pass * kThreads * kBatch + threadIdx.x;
+    unsigned xr[kBatch], xq[kBatch], yr[kBatch], yq[kBatch];
+    bool xok[kBatch], yok[kBatch];
 #pragma unroll
     for (unsigned b = 0; b < kBatch; ++b) {
-      unsigned r, q;
-      if (xs.At(base + b * kThreads, r, q))
-        xv[b] = LoadQuad(x, K, r, d0 + 4 * q);
-      if (ys.At(base + b * kThreads, r, q))
-        yv[b] = LoadQuad(y, K, r, d0 + 4 * q);
+      xok[b] = xs.Valid();
+      xr[b] = xs.Row();
+      xq[b] = xs.Quad();
+      xs.Advance();
+      yok[b] = ys.Valid();
+      yr[b] = ys.Row();
+      yq[b] = ys.Quad();
+      ys.Advance();
+      if (xok[b])
+        xv[b] = LoadQuad(x, K, xr[b], d0 + 4 * xq[b]);
+      if (yok[b])
+        yv[b] = LoadQuad(y, K, yr[b], d0 + 4 * yq[b]);
     }
 #pragma unroll
     for (unsigned b = 0; b < kBatch; ++b) {
-      unsigned r, q;
-      if (xs.At(base + b * kThreads, r, q))
-        Put4<kBf16>(xh, xl, r, 4 * q, xv[b]);
-      if (ys.At(base + b * kThreads, r, q))
-        Put4<kBf16>(yh, yl, r, 4 * q, yv[b]);
+      if (xok[b])
+        Put4<kBf16>(xh, xl, xr[b], 4 * xq[b], xv[b]);
+      if (yok[b])
+        Put4<kBf16>(yh, yl, yr[b], 4 * yq[b], yv[b]);
     }
   }
+}
+
+// Issues the tensor-core steps of depth chunk `chunk` of a product whose
+// operands are staged (hi/lo, or BF16 in the hi parts) and waits for them
+// (bounded). Returns false if the wait timed out.
+template <int KP, bool kSplit>
+__device__ bool MmaChunk(unsigned char *smem, PhaseShared &sh, std::uint32_t &phase,
+                         std::uint32_t tmem, unsigned chunk, bool bf16) {
+  using L = PhaseLayout<KP>;
+  umma::FenceOperands();
+  umma::FenceBeforeSync();
+  __syncthreads();
+  umma::FenceAfterSync();
+  if (threadIdx.x == 0) {
+    const std::uint32_t xh_at = umma::SmemAddress(smem + L::kXh);
+    const std::uint32_t xl_at = umma::SmemAddress(smem + L::kXl);
+    const std::uint32_t yh_at = umma::SmemAddress(smem + L::kYh);
+    const std::uint32_t yl_at = umma::SmemAddress(smem + L::kYl);
+    if (bf16) {
+      constexpr std::uint32_t kBf16 = umma::Bf16Descriptor(128, KP);
+#pragma unroll
+      for (unsigned k = 0; k < kChunk / 16; ++k)
+        umma::MmaBf16(tmem, umma::SmemDescriptor(xh_at + k * 256, kSbo16),
+                      umma::SmemDescriptor(yh_at + k * 256, kSbo16), kBf16,
+                      chunk != 0 || k != 0);
+    } else {
+      constexpr std::uint32_t kTf32 = umma::Tf32Descriptor(128, KP);
+      const std::uint32_t a_parts[3] = {xl_at, xh_at, xh_at};
+      const std::uint32_t b_parts[3] = {yh_at, yl_at, yh_at};
+#pragma unroll
+      for (int part = 0; part < 3; ++part) {
+#pragma unroll
+        for (unsigned k = 0; k < kChunk / 8; ++k) {
+          const std::uint64_t a = umma::SmemDescriptor(a_parts[part] + k * 256, kSbo);
+          const std::uint64_t b = umma::SmemDescriptor(b_parts[part] + k * 256, kSbo);
+          if constexpr (kSplit) {
+            const bool big = part == 2;
+            const std::uint32_t column = big ? chunk * KP : (KP / kChunk) * KP;
+            const bool accumulate = big ? k != 0 : (chunk != 0 || part != 0 || k != 0);
+            umma::MmaTf32(tmem + column, a, b, kTf32, accumulate);
+          } else {
+            umma::MmaTf32(tmem, a, b, kTf32, chunk != 0 || part != 0 || k != 0);
+          }
+        }
+      }
+    }
+    umma::Commit(&sh.barrier);
+  }
+  const bool ok = umma::Wait(&sh.barrier, phase);
+  phase ^= 1u;
+  umma::FenceAfterSync();
+  return ok;
 }
 
 // Tensor-memory lanes 0..127 (one per thread), columns from `tmem`:
@@ -327,48 +411,65 @@ __device__ bool PhaseProduct(unsigned char *smem, PhaseShared &sh, std::uint32_t
       StageChunk<true>(x, y, K, d0, xh, nullptr, yh, nullptr);
     else
       StageChunk<false>(x, y, K, d0, xh, xl, yh, yl);
-    umma::FenceOperands();
-    umma::FenceBeforeSync();
-    __syncthreads();
-    umma::FenceAfterSync();
-    if (threadIdx.x == 0) {
-      const std::uint32_t xh_at = umma::SmemAddress(xh), xl_at = umma::SmemAddress(xl);
-      const std::uint32_t yh_at = umma::SmemAddress(yh), yl_at = umma::SmemAddress(yl);
-      if (bf16) {
-        constexpr std::uint32_t kBf16 = umma::Bf16Descriptor(128, KP);
-#pragma unroll
-        for (unsigned k = 0; k < kChunk / 16; ++k)
-          umma::MmaBf16(tmem, umma::SmemDescriptor(xh_at + k * 256, kSbo16),
-                        umma::SmemDescriptor(yh_at + k * 256, kSbo16), kBf16,
-                        chunk != 0 || k != 0);
-      } else {
-        constexpr std::uint32_t kTf32 = umma::Tf32Descriptor(128, KP);
-        const std::uint32_t a_parts[3] = {xl_at, xh_at, xh_at};
-        const std::uint32_t b_parts[3] = {yh_at, yl_at, yh_at};
-#pragma unroll
-        for (int part = 0; part < 3; ++part) {
-#pragma unroll
-          for (unsigned k = 0; k < kChunk / 8; ++k) {
-            const std::uint64_t a = umma::SmemDescriptor(a_parts[part] + k * 256, kSbo);
-            const std::uint64_t b = umma::SmemDescriptor(b_parts[part] + k * 256, kSbo);
-            if constexpr (kSplit) {
-              const bool big = part == 2;
-              const std::uint32_t column = big ? chunk * KP : (KP / kChunk) * KP;
-              const bool accumulate = big ? k != 0 : (chunk != 0 || part != 0 || k != 0);
-              umma::MmaTf32(tmem + column, a, b, kTf32, accumulate);
-            } else {
-              umma::MmaTf32(tmem, a, b, kTf32, chunk != 0 || part != 0 || k != 0);
-            }
-          }
-        }
-      }
-      umma::Commit(&sh.barrier);
-    }
-    ok = umma::Wait(&sh.barrier, phase) && ok;
-    phase ^= 1u;
-    umma::FenceAfterSync();
+    ok = MmaChunk<KP, kSplit>(smem, sh, phase, tmem, chunk, bf16) && ok;
   }
   return ok;
+}
+
+// Stages depth chunk d0 of one operand (K % 4 == 0), loads batched as in
+// StageChunk.
+template <bool kBf16, class Src>
+__device__ __forceinline__ void StageOne(const Src &src, unsigned K, unsigned d0,
+                                         unsigned char *hi, unsigned char *lo) {
+  const unsigned depth = K - d0 < kChunk ? K - d0 : kChunk;
+  QuadCursor<Src> cursor(K, depth);
+#pragma unroll 1
+  while (cursor.More()) {
+    float4 v[kBatch];
+    unsigned rows[kBatch], quads[kBatch];
+    bool ok[kBatch];
+#pragma unroll
+    for (unsigned b = 0; b < kBatch; ++b) {
+      ok[b] = cursor.Valid();
+      rows[b] = cursor.Row();
+      quads[b] = cursor.Quad();
+      cursor.Advance();
+      if (ok[b])
+        v[b] = LoadQuad(src, K, rows[b], d0 + 4 * quads[b]);
+    }
+#pragma unroll
+    for (unsigned b = 0; b < kBatch; ++b)
+      if (ok[b])
+        Put4<kBf16>(hi, lo, rows[b], 4 * quads[b], v[b]);
+  }
+}
+
+// Y(n, d) = X(d, n) for n, d < K (KP = 64: one depth chunk holds the whole
+// staged operand): copies the staged hi and lo parts (BF16: hi) element by
+// element, so the transpose holds exactly the values staged in X. A warp
+// moves an 8 x 4 block of X per step: its reads cover one core matrix row
+// set (32 distinct banks), its writes two.
+template <bool kBf16>
+__device__ __forceinline__ void TransposeStaged(unsigned K, const unsigned char *xh,
+                                                const unsigned char *xl, unsigned char *yh,
+                                                unsigned char *yl) {
+  const unsigned warp = threadIdx.x / 32, lane = threadIdx.x & 31u;
+  const unsigned row_blocks = (K + 7) / 8, col_blocks = (K + 3) / 4;
+  for (unsigned block = warp; block < row_blocks * col_blocks; block += kThreads / 32) {
+    const unsigned d = (block / col_blocks) * 8 + lane / 4;
+    const unsigned n = (block % col_blocks) * 4 + lane % 4;
+    if (d < K && n < K) {
+      if constexpr (kBf16) {
+        *reinterpret_cast<unsigned short *>(yh + CoreOffset16(n, d)) =
+            *reinterpret_cast<const unsigned short *>(xh + CoreOffset16(d, n));
+      } else {
+        const std::uint32_t from = umma::CoreOffset(d, n, kSbo);
+        const std::uint32_t to = umma::CoreOffset(n, d, kSbo);
+        *reinterpret_cast<float *>(yh + to) = *reinterpret_cast<const float *>(xh + from);
+        *reinterpret_cast<float *>(yl + to) = *reinterpret_cast<const float *>(xl + from);
+      }
+    }
+  }
 }
 
 // One operation of a wide phase kind, executed by the whole CTA.
@@ -460,6 +561,23 @@ template <int KP> struct WideOps {
         *reinterpret_cast<float4 *>(tile + j * TileStride() + c + q) =
             make_float4(row[q], row[q + 1], row[q + 2], row[q + 3]);
   }
+
+  // This thread's walk over the quads of a row-major K x K matrix (K % 4 ==
+  // 0): quad threadIdx.x, then every kThreads-th, as (row, first column).
+  struct TileWalk {
+    unsigned quads, row, column, step_rows, step_quads;
+    __device__ __forceinline__ explicit TileWalk(unsigned K)
+        : quads(K / 4), row(threadIdx.x / (K / 4)), column(4 * (threadIdx.x % (K / 4))),
+          step_rows(kThreads / (K / 4)), step_quads(kThreads % (K / 4)) {}
+    __device__ __forceinline__ void Advance() {
+      row += step_rows;
+      column += 4 * step_quads;
+      if (column >= 4 * quads) {
+        column -= 4 * quads;
+        ++row;
+      }
+    }
+  };
 
   // Rows per warp whose loads are in flight together (MatVec, RakeReverse).
   static constexpr unsigned kRows = KP == 64 ? 8 : 4;
@@ -598,13 +716,10 @@ template <int KP> struct WideOps {
         }
       }
       __syncthreads();
-      const unsigned quads = K / 4;
 #pragma unroll 4
-      for (unsigned f = threadIdx.x; f < K * quads; f += kThreads) {
-        const unsigned r = f / quads, c = 4 * (f % quads);
-        *reinterpret_cast<float4 *>(out + static_cast<std::size_t>(r) * K + c) =
-            *reinterpret_cast<const float4 *>(tile + r * TileStride() + c);
-      }
+      for (TileWalk w(K); w.row < K; w.Advance())
+        *reinterpret_cast<float4 *>(out + static_cast<std::size_t>(w.row) * K + w.column) =
+            *reinterpret_cast<const float4 *>(tile + w.row * TileStride() + w.column);
     } else {
 #pragma unroll 1
       for (unsigned c = 0; c < KP; c += 32) {
@@ -742,12 +857,38 @@ template <int KP> struct WideOps {
     const float *stored = Comps() + static_cast<std::size_t>(i) * KK;
     // P1[r][m] = sum_c R[r][c] right[m][c];  P2[m][c] = sum_r left[r][m] R[r][c].
     const Ratio ratio_of(shift);
-    ok = PhaseProduct<KP, false>(smem, sh, phase, tmem, K, RatioRows{mu, stored, ratio_of},
-                                 Rows{right, nullptr}, a.bf16 != 0) &&
-         ok;
-    ok = PhaseProduct<KP, false>(smem, sh, phase, tmem + KP, K, Columns{left},
-                                 RatioColumns{mu, stored, ratio_of}, a.bf16 != 0) &&
-         ok;
+    if (KP == 64 && K % 4 == 0) {
+      // P1 stages R as its X operand; P2's Y operand is that staged R,
+      // transposed in shared memory, so R is formed once per compression.
+      using L = PhaseLayout<KP>;
+      unsigned char *const xh = smem + L::kXh, *const xl = smem + L::kXl;
+      unsigned char *const yh = smem + L::kYh, *const yl = smem + L::kYl;
+      const bool bf16 = a.bf16 != 0;
+      if (bf16)
+        StageChunk<true>(RatioRows{mu, stored, ratio_of}, Rows{right, nullptr}, K, 0, xh,
+                         nullptr, yh, nullptr);
+      else
+        StageChunk<false>(RatioRows{mu, stored, ratio_of}, Rows{right, nullptr}, K, 0, xh, xl,
+                          yh, yl);
+      ok = MmaChunk<KP, false>(smem, sh, phase, tmem, 0, bf16) && ok;
+      if (bf16)
+        TransposeStaged<true>(K, xh, xl, yh, yl);
+      else
+        TransposeStaged<false>(K, xh, xl, yh, yl);
+      __syncthreads();
+      if (bf16)
+        StageOne<true>(Columns{left}, K, 0, xh, nullptr);
+      else
+        StageOne<false>(Columns{left}, K, 0, xh, xl);
+      ok = MmaChunk<KP, false>(smem, sh, phase, tmem + KP, 0, bf16) && ok;
+    } else {
+      ok = PhaseProduct<KP, false>(smem, sh, phase, tmem, K, RatioRows{mu, stored, ratio_of},
+                                   Rows{right, nullptr}, a.bf16 != 0) &&
+           ok;
+      ok = PhaseProduct<KP, false>(smem, sh, phase, tmem + KP, K, Columns{left},
+                                   RatioColumns{mu, stored, ratio_of}, a.bf16 != 0) &&
+           ok;
+    }
     const std::uint32_t lane_base = tmem + ((threadIdx.x & ~31u) << 16);
     float *left_out = AdjointOf(op.x);
     float *right_out = AdjointOf(op.z);
@@ -756,7 +897,6 @@ template <int KP> struct WideOps {
       // Each product's rows go through the (now idle) operand buffers; the
       // adjoints are then formed and stored in coalesced passes.
       float *tile = reinterpret_cast<float *>(smem);
-      const unsigned quads = K / 4;
       const auto stage_rows = [&](std::uint32_t column) {
 #pragma unroll 1
         for (unsigned c = 0; c < KP; c += 32) {
@@ -770,8 +910,8 @@ template <int KP> struct WideOps {
       // Left adjoint left[r][m] middle[m] P1[r][m].
       stage_rows(0);
 #pragma unroll 4
-      for (unsigned f = threadIdx.x; f < K * quads; f += kThreads) {
-        const unsigned r = f / quads, c = 4 * (f % quads);
+      for (TileWalk w(K); w.row < K; w.Advance()) {
+        const unsigned r = w.row, c = w.column;
         const std::size_t at = static_cast<std::size_t>(r) * K + c;
         const float4 l = *reinterpret_cast<const float4 *>(left + at);
         const float4 p = *reinterpret_cast<const float4 *>(tile + r * TileStride() + c);
@@ -784,8 +924,8 @@ template <int KP> struct WideOps {
       // the middle adjoint (its row sums).
       stage_rows(KP);
 #pragma unroll 4
-      for (unsigned f = threadIdx.x; f < K * quads; f += kThreads) {
-        const unsigned r = f / quads, c = 4 * (f % quads);
+      for (TileWalk w(K); w.row < K; w.Advance()) {
+        const unsigned r = w.row, c = w.column;
         const std::size_t at = static_cast<std::size_t>(r) * K + c;
         const float4 rr = *reinterpret_cast<const float4 *>(right + at);
         float4 *p = reinterpret_cast<float4 *>(tile + r * TileStride() + c);
@@ -874,8 +1014,12 @@ __global__ void __launch_bounds__(kThreads, KP == 64 ? 3 : 1) WidePhaseKernel(Ph
   for (std::uint32_t t = blockIdx.x; t < args.count; t += gridDim.x) {
     const std::uint32_t i = args.offset + t;
     if constexpr (kKind != kPhaseFinish) {
-      if (threadIdx.x == 0 && t + gridDim.x < args.count)
-        ops.template Prefetch<kKind>(i + gridDim.x);
+      if (threadIdx.x == 0) {
+        if (t == blockIdx.x)
+          ops.template Prefetch<kKind>(i);
+        if (t + gridDim.x < args.count)
+          ops.template Prefetch<kKind>(i + gridDim.x);
+      }
     }
     if constexpr (kKind == kPhaseGather)
       ops.Gather(i);
