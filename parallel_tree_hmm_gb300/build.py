@@ -55,6 +55,15 @@ SOURCES = [
     "engine_wide.cu",
     "engine_phase.cu",
     "engine_wide_phase.cu",
+    "engine_phase_groups_32_f64.cu",
+    "engine_phase_groups_32_f32.cu",
+    "engine_phase_groups_28_f32.cu",
+    "engine_phase_groups_24_f32.cu",
+    "engine_phase_groups_20_f32.cu",
+    "engine_phase_groups_16_f64.cu",
+    "engine_phase_groups_16_f32.cu",
+    "engine_phase_groups_8_f64.cu",
+    "engine_phase_groups_8_f32.cu",
     "engine_linear_f32.cu",
     "engine_linear_f64.cu",
     "engine_maximum.cu",

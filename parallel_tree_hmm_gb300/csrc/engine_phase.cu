@@ -96,6 +96,27 @@ cudaError_t LaunchPhase(int scalar_bytes, bool compute_f64, int kind, const Phas
     return scalar_bytes == 4 && !compute_f64 && !args.batch
                ? LaunchWidePhase(kind, args, stream, blocks_per_sm)
                : cudaErrorInvalidValue;
+  if (args.states > 4) {
+    if (args.batch)
+      return cudaErrorInvalidValue;
+    if (args.states <= 8)
+      return compute_f64
+                 ? LaunchGroupPhase8F64(scalar_bytes, kind, args, stream, blocks_per_sm)
+                 : LaunchGroupPhase8F32(scalar_bytes, kind, args, stream, blocks_per_sm);
+    if (args.states <= 16)
+      return compute_f64
+                 ? LaunchGroupPhase16F64(scalar_bytes, kind, args, stream, blocks_per_sm)
+                 : LaunchGroupPhase16F32(scalar_bytes, kind, args, stream, blocks_per_sm);
+    if (compute_f64)
+      return LaunchGroupPhase32F64(scalar_bytes, kind, args, stream, blocks_per_sm);
+    if (args.states <= 20)
+      return LaunchGroupPhase20F32(scalar_bytes, kind, args, stream, blocks_per_sm);
+    if (args.states <= 24)
+      return LaunchGroupPhase24F32(scalar_bytes, kind, args, stream, blocks_per_sm);
+    if (args.states <= 28)
+      return LaunchGroupPhase28F32(scalar_bytes, kind, args, stream, blocks_per_sm);
+    return LaunchGroupPhase32F32(scalar_bytes, kind, args, stream, blocks_per_sm);
+  }
   if (scalar_bytes == 8)
     return compute_f64 ? LaunchTyped<double, double>(kind, args, stream, blocks_per_sm)
                        : LaunchTyped<double, float>(kind, args, stream, blocks_per_sm);

@@ -1,0 +1,11 @@
+// Lane-group phase kernels for padded state count 16, double arithmetic.
+#include "phase_groups_launch.cuh"
+
+namespace thmm {
+
+cudaError_t LaunchGroupPhase16F64(int scalar_bytes, int kind, const PhaseArgs &args,
+                                   cudaStream_t stream, int *blocks_per_sm) {
+  return group_phase::Launch<double, 16>(scalar_bytes, kind, args, stream, blocks_per_sm);
+}
+
+} // namespace thmm

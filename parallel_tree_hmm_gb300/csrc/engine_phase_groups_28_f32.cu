@@ -1,0 +1,12 @@
+// Lane-group phase kernels with register rows of 28 (K in (24, 28]), float
+// arithmetic.
+#include "phase_groups_launch.cuh"
+
+namespace thmm {
+
+cudaError_t LaunchGroupPhase28F32(int scalar_bytes, int kind, const PhaseArgs &args,
+                                   cudaStream_t stream, int *blocks_per_sm) {
+  return group_phase::Launch<float, 28>(scalar_bytes, kind, args, stream, blocks_per_sm);
+}
+
+} // namespace thmm

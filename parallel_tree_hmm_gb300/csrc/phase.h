@@ -1,5 +1,5 @@
-// Level-synchronous phase schedule for small (K <= 4) and wide
-// (32 < K <= 128) state counts.
+// Level-synchronous phase schedule of the sum-product calls (every state
+// count up to 128).
 //
 // The per-tree engine (engine.cuh) contracts one tree per team and walks the
 // tree's plan step by step with a team barrier in between; a tree has 20-50
@@ -174,12 +174,28 @@ PhasePlan BuildPhasePlan(const ProgramSet &set, std::span<const PhaseInstance> i
 // Launches one phase (or reports its occupancy when blocks_per_sm is
 // non-null). scalar_bytes: 4 or 8 (input/output type); compute_f64: FP64
 // arithmetic. Padded state count 4 (K <= 4) runs one thread per operation
-// (phase_engine.cuh); 32 < K <= 128 (FP32 only, forest layout, no tail
-// kinds) one CTA per operation (wide_phase.cuh).
+// (phase_engine.cuh); 4 < K <= 32 (forest layout, no tail kinds) one lane
+// group per operation (phase_groups.cuh); 32 < K <= 128 (FP32 only, forest
+// layout, no tail kinds) one CTA per operation (wide_phase.cuh).
 cudaError_t LaunchPhase(int scalar_bytes, bool compute_f64, int kind, const PhaseArgs &args,
                         cudaStream_t stream, int *blocks_per_sm);
 cudaError_t LaunchWidePhase(int kind, const PhaseArgs &args, cudaStream_t stream,
                             int *blocks_per_sm);
+// 4 < K <= 32: one lane group per operation (phase_groups.cuh), per padded
+// state count and arithmetic type.
+#define THMM_GROUP_PHASE_LAUNCHER(name)                                                    \
+  cudaError_t name(int scalar_bytes, int kind, const PhaseArgs &args, cudaStream_t stream, \
+                   int *blocks_per_sm);
+THMM_GROUP_PHASE_LAUNCHER(LaunchGroupPhase8F32)
+THMM_GROUP_PHASE_LAUNCHER(LaunchGroupPhase8F64)
+THMM_GROUP_PHASE_LAUNCHER(LaunchGroupPhase16F32)
+THMM_GROUP_PHASE_LAUNCHER(LaunchGroupPhase16F64)
+THMM_GROUP_PHASE_LAUNCHER(LaunchGroupPhase32F32)
+THMM_GROUP_PHASE_LAUNCHER(LaunchGroupPhase32F64)
+THMM_GROUP_PHASE_LAUNCHER(LaunchGroupPhase20F32)
+THMM_GROUP_PHASE_LAUNCHER(LaunchGroupPhase24F32)
+THMM_GROUP_PHASE_LAUNCHER(LaunchGroupPhase28F32)
+#undef THMM_GROUP_PHASE_LAUNCHER
 
 // The phase-ordered copy of the observations: ordered[j * items + b] =
 // observations[b * per_item + order[j]] for j < count, b < items (a forest:

@@ -474,13 +474,12 @@ struct Workspace {
     gathers.Upload(set.gathers, stream);
     instances.Upload(table, stream);
     team_order.Upload(order, stream);
-    // Phase schedule of the sum-product calls for up to 4 states and, on
-    // the tensor-core kernels, for 32 < K <= 128. A forest gets records for
+    // Phase schedule of the sum-product calls. A forest gets records for
     // every tree; the batch API (one plan shared by every item, shared edge
     // input) gets, for up to 4 states, the records of one tree, which every
-    // item reads (the shared-topology layout of phase_engine.cuh); above 32
+    // item reads (the shared-topology layout of phase_engine.cuh); above 4
     // states the batch API keeps the per-tree engine.
-    if (PaddedStates(states) == 4 || (states > 32 && !shared_edges)) {
+    if (PaddedStates(states) == 4 || !shared_edges) {
       phase_batch = shared_edges;
       std::vector<PhaseInstance> phase_instances(phase_batch ? 1 : count);
       for (std::size_t i = 0; i < phase_instances.size(); ++i)
@@ -779,14 +778,14 @@ struct Workspace {
   // Rounds of the phase schedule run grid-wide (0: the first round with
   // fewer than 2^17 gathers and compressions); uploads the tail records of
   // the rest. A tail of more than 2^20 trees stays grid-wide, and so do the
-  // batch layout (every item has every round) and the wide-state kinds.
+  // batch layout (every item has every round) and every state count above 4.
   void SetPhaseRounds(std::uint32_t rounds) {
     if (!phase.enabled)
       return;
     std::uint32_t wanted = rounds != 0 ? rounds : phase.AutoTailRound(1u << 17);
     wanted = std::max<std::uint32_t>(wanted, 1);
-    if (phase_batch || states > 32)
-      wanted = phase.rounds; // no tail kinds above 32 states
+    if (phase_batch || states > 4)
+      wanted = phase.rounds; // no tail kinds above 4 states
     PhasePlan::Tail tail;
     if (wanted < phase.rounds) {
       tail = phase.BuildTail(wanted);

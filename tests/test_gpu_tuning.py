@@ -36,15 +36,16 @@ def outputs(view):
     return [np.array(view.log_partitions), np.array(view.nodes), np.array(view.edges)]
 
 
-@pytest.mark.parametrize("states", [4, 8])
+@pytest.mark.parametrize("states", [4, 8, 13, 20, 22, 27, 32])
 def test_tunings_give_identical_marginals(gpu, states):
     rng = np.random.default_rng(40 + states)
     plans, nodes, edges = forest(gpu, rng, states)
     ws = gpu.Workspace()
     ws.reserve_forest(plans, states, kind="marginals", scalar=np.float32)
     model = gpu.BatchedModelView(None, states, len(plans), nodes, edges)
-    # The phase schedule exists for up to 4 states and is then the default.
-    assert ws.tuning["schedule"] == (PHASES if states <= 4 else TEAMS)
+    # The phase schedule is the forest default; above 4 states it has no
+    # tail, so every phase_rounds setting runs all rounds grid-wide.
+    assert ws.tuning["schedule"] == PHASES
     reference = outputs(ws.posterior_marginals_prepared(model))
     settings = [(1, (0, 0, 0, 0)),          # every tree to a CTA team
                 (1 << 31, (0, 0, 0, 0)),    # every tree to a warp team
@@ -56,7 +57,7 @@ def test_tunings_give_identical_marginals(gpu, states):
             ws.set_tuning(threshold, caps, schedule=schedule, phase_rounds=phase_rounds)
             assert ws.tuning["team_threshold"] == threshold
             assert ws.tuning["ctas_per_sm"] == list(caps)
-            assert ws.tuning["schedule"] == (schedule if states <= 4 else TEAMS)
+            assert ws.tuning["schedule"] == schedule
             got = outputs(ws.posterior_marginals_prepared(model))
             for a, b in zip(got, reference):
                 assert np.array_equal(a, b)
@@ -67,6 +68,30 @@ def test_tunings_give_identical_marginals(gpu, states):
     assert ws.tuning["team_threshold"] == chosen["team_threshold"]
     got = outputs(ws.posterior_marginals_prepared(model))
     for a, b in zip(got, reference):
+        assert np.array_equal(a, b)
+
+
+def test_lane_group_phases_replay(gpu):
+    """4 < K <= 32 on the phase schedule (one lane group per operation, no
+    tail): graph replay gives the prepared call's bits, with one launch per
+    kind and round."""
+    rng = np.random.default_rng(78)
+    plans, nodes, edges = forest(gpu, rng, 20)
+    ws = gpu.Workspace()
+    ws.reserve_forest(plans, 20, kind="marginals", scalar=np.float32)
+    rounds = max(p.num_rounds for p in plans)
+    assert ws.tuning["schedule"] == PHASES and ws.tuning["phase_rounds"] == rounds
+    ws.set_tuning(1024, schedule=PHASES, phase_rounds=2)
+    assert ws.tuning["phase_rounds"] == rounds
+    model = gpu.BatchedModelView(None, 20, len(plans), nodes, edges)
+    reference = outputs(ws.posterior_marginals_prepared(model))
+    total = sum(p.num_nodes for p in plans)
+    for _ in range(3):
+        assert ws.enqueue(4) == total
+    ws.synchronize()
+    assert 2 * rounds + 1 <= ws.launches <= 4 * rounds + 1
+    ws.set_tuning(1024, schedule=TEAMS)
+    for a, b in zip(outputs(ws.posterior_marginals_prepared(model)), reference):
         assert np.array_equal(a, b)
 
 
@@ -131,17 +156,18 @@ def test_map_and_sampling_tuning_identical(gpu):
     assert np.array_equal(ws.posterior_sample_prepared(model, uniforms).states, sample_ref)
 
 
-def test_striped_calls_match_single_stripe(gpu):
+@pytest.mark.parametrize("states", [4, 20])
+def test_striped_calls_match_single_stripe(gpu, states):
     """Prepared calls cut into stripes (overlapped copies and kernels) return
     the same bits as one stripe: dense and categorical forests, the batch API
     with shared edges, every operation."""
     rng = np.random.default_rng(11)
-    plans, nodes, edges = forest(gpu, rng, 4)
+    plans, nodes, edges = forest(gpu, rng, states)
     total = sum(p.num_nodes for p in plans)
     uniforms = rng.random(total).astype(np.float32)
     ws = gpu.Workspace()
-    ws.reserve_forest(plans, 4, kind="marginals", scalar=np.float32)
-    model = gpu.BatchedModelView(None, 4, len(plans), nodes, edges)
+    ws.reserve_forest(plans, states, kind="marginals", scalar=np.float32)
+    model = gpu.BatchedModelView(None, states, len(plans), nodes, edges)
     ws.set_tuning(1024, stripes=1, schedule=TEAMS)
     single = outputs(ws.posterior_marginals_prepared(model))
     single_log_z = np.array(ws.log_partition_function_prepared(model).values)
@@ -158,7 +184,7 @@ def test_striped_calls_match_single_stripe(gpu):
                                   single_log_z)
 
     ws2 = gpu.Workspace()
-    ws2.reserve_forest(plans, 4, kind="maximum,sampling", scalar=np.float32)
+    ws2.reserve_forest(plans, states, kind="maximum,sampling", scalar=np.float32)
     ws2.set_tuning(1024, stripes=1)
     map1 = ws2.maximum_a_posteriori_prepared(model)
     map_states, map_weights = np.array(map1.states), np.array(map1.log_weights)
