@@ -76,6 +76,9 @@ def parse_args():
     parser.add_argument("--schedule", choices=["phases", "teams"], default="phases",
                         help="dense workload above 32 states: every round of every tree "
                              "grid-wide (phases) or one CTA per tree (teams)")
+    parser.add_argument("--no-autotune", action="store_true",
+                        help="forest and gw workloads: keep the default launch tuning "
+                             "(a short run, e.g. under a profiler)")
     parser.add_argument("--check-trees", type=int, default=16,
                         help="gw workload: trees checked against the oracle")
     parser.add_argument("--workload", choices=["forest", "gw", "dense"], default="forest",
@@ -390,7 +393,7 @@ def run_ours(args, rank, world, local_rank, dist):
     node_sum = first.nodes.reshape(-1, K).sum(axis=1)
     normalisation_error = float(np.max(np.abs(node_sum - 1.0)))
 
-    tuning = ws.autotune(4, repeats=3)
+    tuning = ws.tuning if args.no_autotune else ws.autotune(4, repeats=3)
 
     def device_time(workspace, steps, warmup, sampler=None):
         ext = torch.cuda.ExternalStream(workspace.stream, device=device)
@@ -426,7 +429,7 @@ def run_ours(args, rank, world, local_rank, dist):
     staged64 = stage(ws64, factor_sets[0])
     staged64.observations[:] = observations
     plain = ws64.posterior_marginals_prepared(staged64, thmm.CategoricalInputUpdate.kAll)
-    plain_tuning = ws64.autotune(4, repeats=2)
+    plain_tuning = ws64.tuning if args.no_autotune else ws64.autotune(4, repeats=2)
     plain_logz_diff = float(np.max(np.abs(plain.log_partitions.astype(np.float64)
                                           - log_z_reference.astype(np.float64))
                                    / np.maximum(1.0, np.abs(plain.log_partitions))))
@@ -721,8 +724,8 @@ def run_gw(args, rank, world, local_rank, dist):
         node0 += n
     agreements = {key: agreement.merge(value) for key, value in parts.items()}
 
-    tuning_map = ws.autotune(2, repeats=2)
-    tuning_sample = ws.autotune(3, repeats=2)
+    tuning_map = ws.tuning if args.no_autotune else ws.autotune(2, repeats=2)
+    tuning_sample = ws.tuning if args.no_autotune else ws.autotune(3, repeats=2)
 
     def step():
         ws.enqueue(2)
