@@ -377,16 +377,19 @@ thmm_status thmm_device_inputs_ready(thmm_workspace *workspace, size_t batch);
  * cut into `stripes` (1 to 8; 0: one per 2 Mi nodes) contiguous runs of
  * instances whose input copies, kernels and output copies overlap.
  * `schedule` picks how sum-product calls (partition, log partition,
- * marginals) are scheduled when the workspace has up to 4 states:
- * THMM_SCHEDULE_TEAMS contracts each tree with one CTA or warp walking its
- * plan step by step; THMM_SCHEDULE_PHASES runs each round of every tree in
- * one grid-wide launch per operation kind (the default where available).
- * Other workspaces always use THMM_SCHEDULE_TEAMS. Under
- * THMM_SCHEDULE_PHASES, the first `phase_rounds` rounds run as grid-wide
- * launches and the remaining rounds of each tree of a forest run in one warp
- * per tree (0: chosen from the operation counts; at least the tree's round
- * count: every round grid-wide; the batch API's shared-topology layout runs
- * every round grid-wide). No setting changes any result bit. */
+ * marginals) are scheduled: THMM_SCHEDULE_TEAMS contracts each tree with one
+ * CTA or warp walking its plan step by step; THMM_SCHEDULE_PHASES runs each
+ * round of every tree in one grid-wide launch per operation kind (the
+ * default where available: forests at every state count, and the batch API
+ * up to 4 states; the batch API above 4 states always uses
+ * THMM_SCHEDULE_TEAMS). Under THMM_SCHEDULE_PHASES with up to 4 states, the
+ * first `phase_rounds` rounds run as grid-wide launches and the remaining
+ * rounds of each tree of a forest run in one warp per tree (0: chosen from
+ * the operation counts; at least the tree's round count: every round
+ * grid-wide); the batch API's shared-topology layout and every workspace
+ * above 4 states run every round grid-wide. Up to 32 states no setting
+ * changes any result bit; above 32 the two schedules round the tensor-core
+ * products differently (both within the same bounds of FP64). */
 #define THMM_SCHEDULE_TEAMS 0
 #define THMM_SCHEDULE_PHASES 1
 typedef struct thmm_tuning {
