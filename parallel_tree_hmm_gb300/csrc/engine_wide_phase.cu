@@ -20,7 +20,7 @@ cudaError_t LaunchWideKind(const PhaseArgs &args, cudaStream_t stream, int *bloc
   if (status != cudaSuccess)
     return status;
   int per_sm = 0;
-  status = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, wide::kThreads, smem);
+  status = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, L::kThreads, smem);
   if (status != cudaSuccess || blocks_per_sm != nullptr) {
     if (blocks_per_sm != nullptr)
       *blocks_per_sm = per_sm;
@@ -41,7 +41,7 @@ cudaError_t LaunchWideKind(const PhaseArgs &args, cudaStream_t stream, int *bloc
   const std::uint64_t slots =
       static_cast<std::uint64_t>(sms) * static_cast<std::uint64_t>(per_sm > 0 ? per_sm : 1);
   const unsigned grid = static_cast<unsigned>(args.count < slots ? args.count : slots);
-  kernel<<<grid, wide::kThreads, smem, stream>>>(args);
+  kernel<<<grid, L::kThreads, smem, stream>>>(args);
   return cudaGetLastError();
 }
 

@@ -45,6 +45,10 @@ namespace wide {
 // state count KP: operand parts of KP rows x a depth chunk of 64 (hi, lo of
 // X, then of Y; BF16 uses the hi parts only), then the K-vectors.
 template <int KP> struct PhaseLayout {
+  // Threads per CTA: 128 at KP = 64 (three CTAs per SM), 256 at KP = 128
+  // (one CTA per SM, so twice the warps for staging and epilogues; warps w
+  // and w + 4 share TMEM lane quarter w and split the columns).
+  static constexpr unsigned kThreads = KP == 64 ? 128u : 256u;
   static constexpr unsigned kPart = KP * kChunk * 4;
   static constexpr unsigned kXh = 0, kXl = kPart, kYh = 2 * kPart, kYl = 3 * kPart;
   static constexpr unsigned kVectorsAt = 4 * kPart;
@@ -76,17 +80,17 @@ struct PhaseShared {
   double root_sum;
   std::uint32_t tmem;
   int root_finite;
-  float reduce[kThreads / 32];
+  float reduce[8]; // one per warp (at most 256 threads)
 };
 
-__device__ __forceinline__ float CtaMax(float v, PhaseShared &sh) {
+template <unsigned T> __device__ __forceinline__ float CtaMax(float v, PhaseShared &sh) {
   v = WarpMax(v);
   if ((threadIdx.x & 31) == 0)
     sh.reduce[threadIdx.x / 32] = v;
   __syncthreads();
   float m = sh.reduce[0];
 #pragma unroll
-  for (unsigned w = 1; w < kThreads / 32; ++w)
+  for (unsigned w = 1; w < T / 32; ++w)
     m = m < sh.reduce[w] ? sh.reduce[w] : m;
   __syncthreads();
   return m;
@@ -188,12 +192,12 @@ struct RatioColumns {
 constexpr unsigned kBatch = 4;
 
 // This thread's walk over the quad slots of an operand chunk: slot
-// threadIdx.x, then every kThreads-th. The row and quad of each slot are
+// threadIdx.x, then every T-th. The row and quad of each slot are
 // advanced incrementally (one division when the walk starts, none per slot).
 //   * Row sources: slot idx is lane t = idx % 32 of group g = idx / 32, row
 //     (g / quad_groups) * 8 + t % 8, quad (g % quad_groups) * 4 + t / 8;
 //   * column sources: row idx % K, quad idx / K.
-template <class Src> struct QuadCursor {
+template <class Src, unsigned T> struct QuadCursor {
   unsigned K, quads, quad_groups;
   unsigned major, minor; // rows: g / quad_groups, g % quad_groups; columns: q, r
   unsigned step_major, step_minor;
@@ -203,15 +207,15 @@ template <class Src> struct QuadCursor {
     if constexpr (Src::kColumns) {
       major = threadIdx.x / K;
       minor = threadIdx.x % K;
-      step_major = kThreads / K;
-      step_minor = kThreads % K;
+      step_major = T / K;
+      step_minor = T % K;
       lane_row = lane_quad = 0;
     } else {
       const unsigned g = threadIdx.x >> 5, t = threadIdx.x & 31u;
       major = g / quad_groups;
       minor = g % quad_groups;
-      step_major = (kThreads / 32) / quad_groups;
-      step_minor = (kThreads / 32) % quad_groups;
+      step_major = (T / 32) / quad_groups;
+      step_minor = (T / 32) % quad_groups;
       lane_row = t & 7u;
       lane_quad = t >> 3;
     }
@@ -268,21 +272,21 @@ __device__ __forceinline__ void Put4(unsigned char *hi, unsigned char *lo, unsig
 }
 
 // Clears depths [depth, kChunk) of rows < K (a later, shorter chunk).
-template <bool kBf16>
+template <bool kBf16, unsigned T>
 __device__ __forceinline__ void ClearTail(unsigned K, unsigned depth, unsigned char *hi,
                                           unsigned char *lo) {
   const unsigned pad = kChunk - depth;
-  for (unsigned idx = threadIdx.x; idx < K * pad; idx += kThreads)
+  for (unsigned idx = threadIdx.x; idx < K * pad; idx += T)
     Put<kBf16>(hi, lo, idx / pad, depth + idx % pad, 0.0f);
 }
 
 // Any K: one element per slot (used when K % 4 != 0).
-template <bool kBf16, class Src>
+template <bool kBf16, unsigned T, class Src>
 __device__ __forceinline__ void StageScalar(const Src &src, unsigned K, unsigned d0,
                                             unsigned depth, unsigned char *hi,
                                             unsigned char *lo) {
 #pragma unroll 4
-  for (unsigned idx = threadIdx.x; idx < K * depth; idx += kThreads) {
+  for (unsigned idx = threadIdx.x; idx < K * depth; idx += T) {
     const unsigned r = Src::kColumns ? idx % K : idx / depth;
     const unsigned d = Src::kColumns ? idx / K : idx % depth;
     Put<kBf16>(hi, lo, r, d, src.At(K, r, d0 + d));
@@ -290,22 +294,22 @@ __device__ __forceinline__ void StageScalar(const Src &src, unsigned K, unsigned
 }
 
 // Stages depth chunk d0 of both operands of a product.
-template <bool kBf16, class XS, class YS>
+template <bool kBf16, unsigned T, class XS, class YS>
 __device__ __forceinline__ void StageChunk(const XS &x, const YS &y, unsigned K, unsigned d0,
                                            unsigned char *xh, unsigned char *xl,
                                            unsigned char *yh, unsigned char *yl) {
   const unsigned depth = K - d0 < kChunk ? K - d0 : kChunk;
   if (d0 != 0 && depth < kChunk) {
-    ClearTail<kBf16>(K, depth, xh, xl);
-    ClearTail<kBf16>(K, depth, yh, yl);
+    ClearTail<kBf16, T>(K, depth, xh, xl);
+    ClearTail<kBf16, T>(K, depth, yh, yl);
   }
   if (K % 4 != 0) {
-    StageScalar<kBf16>(x, K, d0, depth, xh, xl);
-    StageScalar<kBf16>(y, K, d0, depth, yh, yl);
+    StageScalar<kBf16, T>(x, K, d0, depth, xh, xl);
+    StageScalar<kBf16, T>(y, K, d0, depth, yh, yl);
     return;
   }
-  QuadCursor<XS> xs(K, depth);
-  QuadCursor<YS> ys(K, depth);
+  QuadCursor<XS, T> xs(K, depth);
+  QuadCursor<YS, T> ys(K, depth);
 #pragma unroll 1
   while (xs.More() || ys.More()) {
     float4 xv[kBatch], yv[kBatch];
@@ -407,10 +411,11 @@ __device__ bool PhaseProduct(unsigned char *smem, PhaseShared &sh, std::uint32_t
 #pragma unroll 1
   for (unsigned chunk = 0; chunk < KP / kChunk; ++chunk) {
     const unsigned d0 = chunk * kChunk;
+    constexpr unsigned T = L::kThreads;
     if (bf16)
-      StageChunk<true>(x, y, K, d0, xh, nullptr, yh, nullptr);
+      StageChunk<true, T>(x, y, K, d0, xh, nullptr, yh, nullptr);
     else
-      StageChunk<false>(x, y, K, d0, xh, xl, yh, yl);
+      StageChunk<false, T>(x, y, K, d0, xh, xl, yh, yl);
     ok = MmaChunk<KP, kSplit>(smem, sh, phase, tmem, chunk, bf16) && ok;
   }
   return ok;
@@ -418,11 +423,11 @@ __device__ bool PhaseProduct(unsigned char *smem, PhaseShared &sh, std::uint32_t
 
 // Stages depth chunk d0 of one operand (K % 4 == 0), loads batched as in
 // StageChunk.
-template <bool kBf16, class Src>
+template <bool kBf16, unsigned T, class Src>
 __device__ __forceinline__ void StageOne(const Src &src, unsigned K, unsigned d0,
                                          unsigned char *hi, unsigned char *lo) {
   const unsigned depth = K - d0 < kChunk ? K - d0 : kChunk;
-  QuadCursor<Src> cursor(K, depth);
+  QuadCursor<Src, T> cursor(K, depth);
 #pragma unroll 1
   while (cursor.More()) {
     float4 v[kBatch];
@@ -449,13 +454,13 @@ __device__ __forceinline__ void StageOne(const Src &src, unsigned K, unsigned d0
 // element, so the transpose holds exactly the values staged in X. A warp
 // moves an 8 x 4 block of X per step: its reads cover one core matrix row
 // set (32 distinct banks), its writes two.
-template <bool kBf16>
+template <bool kBf16, unsigned T>
 __device__ __forceinline__ void TransposeStaged(unsigned K, const unsigned char *xh,
                                                 const unsigned char *xl, unsigned char *yh,
                                                 unsigned char *yl) {
   const unsigned warp = threadIdx.x / 32, lane = threadIdx.x & 31u;
   const unsigned row_blocks = (K + 7) / 8, col_blocks = (K + 3) / 4;
-  for (unsigned block = warp; block < row_blocks * col_blocks; block += kThreads / 32) {
+  for (unsigned block = warp; block < row_blocks * col_blocks; block += T / 32) {
     const unsigned d = (block / col_blocks) * 8 + lane / 4;
     const unsigned n = (block % col_blocks) * 4 + lane % 4;
     if (d < K && n < K) {
@@ -474,6 +479,12 @@ __device__ __forceinline__ void TransposeStaged(unsigned K, const unsigned char 
 
 // One operation of a wide phase kind, executed by the whole CTA.
 template <int KP> struct WideOps {
+  // Threads of the CTA; a thread's TMEM lane (accumulator row) is
+  // threadIdx.x % 128, and with 256 threads the two halves of the CTA take
+  // the two halves of the columns.
+  static constexpr unsigned kThreads = PhaseLayout<KP>::kThreads;
+  static constexpr unsigned kHalves = kThreads / 128;
+  static constexpr unsigned kHalfColumns = KP / kHalves;
   const PhaseArgs &a;
   PhaseShared &sh;
   unsigned char *smem;
@@ -663,10 +674,10 @@ template <int KP> struct WideOps {
       MatVec(PathPtr(rake.x), leaf, msg);
       __syncthreads();
       const float message = j < K ? msg[j] : 0.0f;
-      int s = ExponentOf(CtaMax(message, sh));
+      int s = ExponentOf(CtaMax<kThreads>(message, sh));
       e += s;
       const float value = j < K ? v[j] * ScalePow2(message, -s) : 0.0f;
-      s = ExponentOf(CtaMax(value, sh));
+      s = ExponentOf(CtaMax<kThreads>(value, sh));
       e += s;
       if (j < K)
         v[j] = ScalePow2(value, -s);
@@ -682,37 +693,38 @@ template <int KP> struct WideOps {
   // power of two of its largest entry.
   __device__ void Compress(std::uint32_t i) {
     const uint4 op = a.compress[i];
-    const unsigned j = threadIdx.x;
     const int e = PathExp(op.x) + PathExp(op.z) + NodeInto(op.y, op.w, middle);
     __syncthreads();
     ok = PhaseProduct<KP, true>(smem, sh, phase, tmem, K, Rows{PathPtr(op.x), middle},
                                 Columns{PathPtr(op.z)}, a.bf16 != 0) &&
          ok;
-    const std::uint32_t lane_base = tmem + ((threadIdx.x & ~31u) << 16);
+    // Accumulator row `row` (TMEM lane), columns [c0, c0 + kHalfColumns).
+    const unsigned row = threadIdx.x % 128, c0 = (threadIdx.x / 128) * kHalfColumns;
+    const std::uint32_t lane_base = tmem + ((row & ~31u) << 16);
     float m = 0.0f;
 #pragma unroll 1
-    for (unsigned c = 0; c < KP; c += 32) {
-      float row[32];
-      SplitSum32<KP>(lane_base, c, row, a.bf16 != 0);
+    for (unsigned c = c0; c < c0 + kHalfColumns; c += 32) {
+      float values[32];
+      SplitSum32<KP>(lane_base, c, values, a.bf16 != 0);
 #pragma unroll
       for (unsigned q = 0; q < 32; ++q)
-        if (j < K && c + q < K)
-          m = m < row[q] ? row[q] : m;
+        if (row < K && c + q < K)
+          m = m < values[q] ? values[q] : m;
     }
-    const int s = ExponentOf(CtaMax(m, sh));
+    const int s = ExponentOf(CtaMax<kThreads>(m, sh));
     float *out = Comps() + static_cast<std::size_t>(i) * KK;
     if (K % 4 == 0) {
       // Rows through the (now idle) operand buffers, then coalesced stores.
       float *tile = reinterpret_cast<float *>(smem);
 #pragma unroll 1
-      for (unsigned c = 0; c < KP; c += 32) {
-        float row[32];
-        SplitSum32<KP>(lane_base, c, row, a.bf16 != 0);
-        if (j < K) {
+      for (unsigned c = c0; c < c0 + kHalfColumns; c += 32) {
+        float values[32];
+        SplitSum32<KP>(lane_base, c, values, a.bf16 != 0);
+        if (row < K) {
 #pragma unroll
           for (unsigned q = 0; q < 32; ++q)
-            row[q] = ScalePow2(row[q], -s);
-          TileRow(tile, j, c, row);
+            values[q] = ScalePow2(values[q], -s);
+          TileRow(tile, row, c, values);
         }
       }
       __syncthreads();
@@ -722,18 +734,18 @@ template <int KP> struct WideOps {
             *reinterpret_cast<const float4 *>(tile + w.row * TileStride() + w.column);
     } else {
 #pragma unroll 1
-      for (unsigned c = 0; c < KP; c += 32) {
-        float row[32];
-        SplitSum32<KP>(lane_base, c, row, a.bf16 != 0);
-        if (j < K) {
+      for (unsigned c = c0; c < c0 + kHalfColumns; c += 32) {
+        float values[32];
+        SplitSum32<KP>(lane_base, c, values, a.bf16 != 0);
+        if (row < K) {
 #pragma unroll
           for (unsigned q = 0; q < 32; ++q)
             if (c + q < K)
-              out[static_cast<std::size_t>(j) * K + c + q] = ScalePow2(row[q], -s);
+              out[static_cast<std::size_t>(row) * K + c + q] = ScalePow2(values[q], -s);
         }
       }
     }
-    if (j == 0)
+    if (threadIdx.x == 0)
       a.comp_exp[i] = e + s;
     umma::FenceBeforeSync();
     __syncthreads();
@@ -865,21 +877,21 @@ template <int KP> struct WideOps {
       unsigned char *const yh = smem + L::kYh, *const yl = smem + L::kYl;
       const bool bf16 = a.bf16 != 0;
       if (bf16)
-        StageChunk<true>(RatioRows{mu, stored, ratio_of}, Rows{right, nullptr}, K, 0, xh,
-                         nullptr, yh, nullptr);
+        StageChunk<true, kThreads>(RatioRows{mu, stored, ratio_of}, Rows{right, nullptr}, K, 0,
+                                   xh, nullptr, yh, nullptr);
       else
-        StageChunk<false>(RatioRows{mu, stored, ratio_of}, Rows{right, nullptr}, K, 0, xh, xl,
-                          yh, yl);
+        StageChunk<false, kThreads>(RatioRows{mu, stored, ratio_of}, Rows{right, nullptr}, K, 0,
+                                    xh, xl, yh, yl);
       ok = MmaChunk<KP, false>(smem, sh, phase, tmem, 0, bf16) && ok;
       if (bf16)
-        TransposeStaged<true>(K, xh, xl, yh, yl);
+        TransposeStaged<true, kThreads>(K, xh, xl, yh, yl);
       else
-        TransposeStaged<false>(K, xh, xl, yh, yl);
+        TransposeStaged<false, kThreads>(K, xh, xl, yh, yl);
       __syncthreads();
       if (bf16)
-        StageOne<true>(Columns{left}, K, 0, xh, nullptr);
+        StageOne<true, kThreads>(Columns{left}, K, 0, xh, nullptr);
       else
-        StageOne<false>(Columns{left}, K, 0, xh, xl);
+        StageOne<false, kThreads>(Columns{left}, K, 0, xh, xl);
       ok = MmaChunk<KP, false>(smem, sh, phase, tmem + KP, 0, bf16) && ok;
     } else {
       ok = PhaseProduct<KP, false>(smem, sh, phase, tmem, K, RatioRows{mu, stored, ratio_of},
@@ -889,7 +901,9 @@ template <int KP> struct WideOps {
                                    RatioColumns{mu, stored, ratio_of}, a.bf16 != 0) &&
            ok;
     }
-    const std::uint32_t lane_base = tmem + ((threadIdx.x & ~31u) << 16);
+    // Accumulator row `row` (TMEM lane), columns [c0, c0 + kHalfColumns).
+    const unsigned row = threadIdx.x % 128, c0 = (threadIdx.x / 128) * kHalfColumns;
+    const std::uint32_t lane_base = tmem + ((row & ~31u) << 16);
     float *left_out = AdjointOf(op.x);
     float *right_out = AdjointOf(op.z);
     float total = 0.0f;
@@ -899,11 +913,11 @@ template <int KP> struct WideOps {
       float *tile = reinterpret_cast<float *>(smem);
       const auto stage_rows = [&](std::uint32_t column) {
 #pragma unroll 1
-        for (unsigned c = 0; c < KP; c += 32) {
-          float row[32];
-          umma::Load32(lane_base + column + c, row);
-          if (j < K)
-            TileRow(tile, j, c, row);
+        for (unsigned c = c0; c < c0 + kHalfColumns; c += 32) {
+          float values[32];
+          umma::Load32(lane_base + column + c, values);
+          if (row < K)
+            TileRow(tile, row, c, values);
         }
         __syncthreads();
       };
@@ -938,9 +952,9 @@ template <int KP> struct WideOps {
       }
       __syncthreads();
       if (j < K) {
-        const float *row = tile + j * TileStride();
+        const float *row_values = tile + j * TileStride();
         for (unsigned c = 0; c < K; c += 4) {
-          const float4 v = *reinterpret_cast<const float4 *>(row + c);
+          const float4 v = *reinterpret_cast<const float4 *>(row_values + c);
           total += v.x;
           total += v.y;
           total += v.z;
@@ -948,36 +962,47 @@ template <int KP> struct WideOps {
         }
       }
     } else {
-      // (tcgen05.ld is warp-collective: every lane loads, lanes j >= K discard.)
-      const float *left_row = left + static_cast<std::size_t>(j) * K;
-      const float *right_row = right + static_cast<std::size_t>(j) * K;
-      const float middle_j = j < K ? middle[j] : 0.0f;
+      // Row-per-thread stores (tcgen05.ld is warp-collective: every lane
+      // loads, rows >= K discard). The halves' partial middle adjoints meet
+      // in the msg and ratio vectors.
+      const float *left_row = left + static_cast<std::size_t>(row) * K;
+      const float *right_row = right + static_cast<std::size_t>(row) * K;
+      const float middle_row = row < K ? middle[row] : 0.0f;
 #pragma unroll 1
-      for (unsigned c = 0; c < KP; c += 32) {
+      for (unsigned c = c0; c < c0 + kHalfColumns; c += 32) {
         float p1[32];
         umma::Load32(lane_base + c, p1);
-        if (j < K) {
+        if (row < K) {
 #pragma unroll
           for (unsigned q = 0; q < 32; ++q)
             if (c + q < K)
-              left_out[static_cast<std::size_t>(j) * K + c + q] =
+              left_out[static_cast<std::size_t>(row) * K + c + q] =
                   left_row[c + q] * middle[c + q] * p1[q];
         }
       }
+      float partial = 0.0f;
 #pragma unroll 1
-      for (unsigned c = 0; c < KP; c += 32) {
+      for (unsigned c = c0; c < c0 + kHalfColumns; c += 32) {
         float p2[32];
         umma::Load32(lane_base + KP + c, p2);
-        if (j < K) {
+        if (row < K) {
 #pragma unroll
           for (unsigned q = 0; q < 32; ++q) {
             if (c + q < K) {
-              const float adjoint = right_row[c + q] * middle_j * p2[q];
-              right_out[static_cast<std::size_t>(j) * K + c + q] = adjoint;
-              total += adjoint;
+              const float adjoint = right_row[c + q] * middle_row * p2[q];
+              right_out[static_cast<std::size_t>(row) * K + c + q] = adjoint;
+              partial += adjoint;
             }
           }
         }
+      }
+      if (kHalves == 1) {
+        total = partial;
+      } else {
+        (threadIdx.x < 128 ? msg : ratio)[row] = partial;
+        __syncthreads();
+        if (j < K)
+          total = msg[j] + ratio[j];
       }
     }
     if (j < K)
@@ -990,7 +1015,8 @@ template <int KP> struct WideOps {
 // One kind of one round over operations [offset, offset + count): a
 // persistent grid, CTA b taking operations b, b + grid, ...
 template <int KP, int kKind>
-__global__ void __launch_bounds__(kThreads, KP == 64 ? 3 : 1) WidePhaseKernel(PhaseArgs args) {
+__global__ void __launch_bounds__(PhaseLayout<KP>::kThreads, KP == 64 ? 3 : 1)
+    WidePhaseKernel(PhaseArgs args) {
   constexpr bool kTensor = kKind == kPhaseCompress || kKind == kPhaseCompressReverse;
   using L = PhaseLayout<KP>;
   extern __shared__ __align__(1024) unsigned char dynamic_smem[];
@@ -1000,7 +1026,7 @@ __global__ void __launch_bounds__(kThreads, KP == 64 ? 3 : 1) WidePhaseKernel(Ph
   bool ok = true;
   if constexpr (kTensor) {
     float4 *p = reinterpret_cast<float4 *>(dynamic_smem);
-    for (unsigned i = threadIdx.x; i < L::kVectorsAt / 16; i += kThreads)
+    for (unsigned i = threadIdx.x; i < L::kVectorsAt / 16; i += L::kThreads)
       p[i] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
     if (threadIdx.x == 0)
       umma::BarrierInit(&sh.barrier);
