@@ -76,6 +76,9 @@ def parse_args():
     parser.add_argument("--schedule", choices=["phases", "teams"], default="phases",
                         help="dense workload above 32 states: every round of every tree "
                              "grid-wide (phases) or one CTA per tree (teams)")
+    parser.add_argument("--phase-rounds", type=int, default=None,
+                        help="forest workload with --no-autotune: grid-wide rounds of the "
+                             "phase schedule (0 automatic)")
     parser.add_argument("--no-autotune", action="store_true",
                         help="forest and gw workloads: keep the default launch tuning "
                              "(a short run, e.g. under a profiler)")
@@ -393,6 +396,8 @@ def run_ours(args, rank, world, local_rank, dist):
     node_sum = first.nodes.reshape(-1, K).sum(axis=1)
     normalisation_error = float(np.max(np.abs(node_sum - 1.0)))
 
+    if args.no_autotune and args.phase_rounds is not None:
+        ws.set_tuning(ws.tuning["team_threshold"], phase_rounds=args.phase_rounds)
     tuning = ws.tuning if args.no_autotune else ws.autotune(4, repeats=3)
 
     def device_time(workspace, steps, warmup, sampler=None):

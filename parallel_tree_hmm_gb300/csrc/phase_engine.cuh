@@ -426,11 +426,27 @@ template <typename Scalar, typename Compute, class Index> struct PhaseOps {
 // Tail rounds of one tree per warp (kPhaseTailForward / kPhaseTailReverse):
 // the lanes take the operations of a step in turn, with a warp barrier
 // (which also orders the lanes' global-memory accesses) between steps.
+// Starts moving `count` 16-byte records from `p` into L2 (a hint).
+__device__ __forceinline__ void PrefetchRecords(const void *p, std::uint32_t count) {
+  if (count != 0)
+    asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(p), "r"(count * 16u)
+                 : "memory");
+}
+
 template <typename Scalar, typename Compute, bool kReverse>
 __device__ __forceinline__ void TailTree(const PhaseOps<Scalar, Compute, ForestIndex> &ops,
                                          const PhaseArgs &a, std::uint32_t item) {
   const unsigned lane = threadIdx.x & 31u;
   const uint4 tree = a.tail_items[item];
+  // The walk below is a chain of dependent loads per round; first bring
+  // every tail round's records of this tree into L2 (lane e: round e).
+  for (std::uint32_t e = lane; e < tree.z; e += 32) {
+    const uint4 round = a.tail_rounds[tree.y + e];
+    const uint2 rakes = a.tail_rakes[tree.y + e];
+    PrefetchRecords(a.gathers + round.x, round.y);
+    PrefetchRecords(a.compress + round.z, round.w);
+    PrefetchRecords(a.rakes + rakes.x, rakes.y);
+  }
   for (std::uint32_t e = 0; e < tree.z; ++e) {
     const std::uint32_t at = tree.y + (kReverse ? tree.z - 1 - e : e);
     const uint4 round = a.tail_rounds[at];
