@@ -19,7 +19,7 @@
 
 namespace thmm {
 
-constexpr int kPhaseThreads = 256;
+constexpr int kPhaseThreads = 128;
 
 // Where the operands of one operation live. Forest layout: the records hold
 // absolute indices of every tree's nodes, edges and compressions, so every
