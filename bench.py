@@ -4,8 +4,10 @@ gradient of log Z) over an uneven forest, on GB300.
 Workloads (--workload): `forest` (default, below); `gw`: Galton-Watson
 forest, K = 8, MAP + posterior sampling; `dense`: dense lognormal factors,
 spine-heavy trees at K = 64/128 on the tensor-core engine, or with --shape
-recursive --states 20 --tree-nodes 5000 the differentiation workload. Every
-workload autotunes the launch (thmm_autotune) before timing; the timed device
+recursive --states 20 --tree-nodes 5000 the differentiation workload;
+`sites`: the reference's batch API on one binary tree with many sites
+(phylogenetic-style, the shared-topology layout). The forest and gw
+workloads autotune the launch (thmm_autotune) before timing; the timed device
 steps replay a CUDA graph (thmm_enqueue); prepared calls overlap copies and
 kernels in stripes.
 
@@ -84,7 +86,10 @@ def parse_args():
                              "(a short run, e.g. under a profiler)")
     parser.add_argument("--check-trees", type=int, default=16,
                         help="gw workload: trees checked against the oracle")
-    parser.add_argument("--workload", choices=["forest", "gw", "dense"], default="forest",
+    parser.add_argument("--sites", type=int, default=4096,
+                        help="sites workload: batch items (sites) sharing the tree")
+    parser.add_argument("--workload", choices=["forest", "gw", "dense", "sites"],
+                        default="forest",
                         help="forest: uneven forest, marginals (default); gw: "
                              "Galton-Watson forest, MAP + posterior sampling; dense: "
                              "spine-heavy trees, K = 64 or 128, tensor-core marginals")
@@ -288,6 +293,8 @@ def main():
         run_gw(args, rank, world, local_rank, dist)
     elif args.workload == "dense":
         run_dense(args, rank, world, local_rank, dist)
+    elif args.workload == "sites":
+        run_sites(args, rank, world, local_rank, dist)
     elif args.impl == "reference":
         run_reference(args, rank, world, dist)
     else:
@@ -1013,6 +1020,141 @@ def run_dense(args, rank, world, local_rank, dist):
     }
     if cpu is not None:
         line["cpu_baseline"] = cpu
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+
+
+def run_sites(args, rank, world, local_rank, dist):
+    """Phylogenetic-style batch through the reference's batch API: ONE random
+    binary tree (leaf splitting, --tree-nodes, default 2001 nodes) and
+    --sites node-factor sets (sites) sharing its edge factors; K=4, leaf
+    observations uniform over 4 categories, a Dirichlet(5) emission table,
+    Dirichlet(1) root and edge rows; log Z and node/edge marginals per site.
+    The shared-topology layout reads each edge row once per warp of 32 sites,
+    so the step reads the edge factors from DRAM once (edge_bytes_read) where
+    a per-site layout would read them once per site (edge_bytes_per_site)."""
+    import torch
+
+    import parallel_tree_hmm_gb300 as thmm
+    from oracle import bridge
+    from parallel_tree_hmm_gb300 import synthetic
+
+    K, B = 4, args.sites
+    rng = np.random.default_rng(rank_seed(args.seed, rank))
+    parents = synthetic.leaf_splitting(rng, args.tree_nodes or 2001)
+    cpu_plan = bridge.CpuPlan(parents)
+    observed = synthetic.leaves(parents)
+    n, e, leaves = cpu_plan.num_nodes, cpu_plan.num_edges, len(observed)
+    root = synthetic.dirichlet_rows(rng, 1, K, 1.0, np.float32).ravel()
+    emission = synthetic.dirichlet_rows(rng, K, K, 5.0, np.float32).ravel()
+    edges = synthetic.stochastic_edges(rng, e, K, 1.0, np.float32)
+    observations = rng.integers(0, K, B * leaves).astype(np.uint8)
+
+    # FP64 oracle on a sample of sites (the CPU baseline, and the reference arm).
+    sample = min(B, 256)
+    obs = observations.reshape(B, leaves)
+    emit = emission.reshape(K, K).astype(np.float64)
+    root_node = int(np.flatnonzero(np.asarray(parents) < 0)[0])
+
+    def site(b):
+        dense = np.ones((n, K))
+        dense[root_node] = root
+        dense[observed] = dense[observed] * emit[obs[b]]
+        z, _, _, _ = bridge.marginals(cpu_plan, K, dense.ravel(), edges.astype(np.float64))
+        return z
+
+    if rank != 0 and args.impl == "reference":
+        return
+    start = time.perf_counter()
+    with concurrent.futures.ThreadPoolExecutor(os.cpu_count() or 1) as pool:
+        oracle_z = list(pool.map(site, range(sample)))
+    cpu_s = time.perf_counter() - start
+    cpu = {"value": sample * n / cpu_s, "unit": UNIT, "cores": os.cpu_count() or 1,
+           "kind": "port", "sample": f"{sample} sites, FP64 log-domain marginals, {cpu_s:.2f} s"}
+    metric = "tree-nodes/s for logZ+marginals+grad (batch API, one tree, many sites)"
+    config = {"workload": (f"phylogenetic-style batch: one random binary tree of {n} "
+                           f"nodes ({leaves} observed leaves), {B} sites, K={K}, "
+                           f"kAll marginals through the batch API"),
+              "sites": B, "tree_nodes": n, "states": K}
+    if args.impl == "reference":
+        print(json.dumps({
+            "impl": "reference", "metric": metric, "value": cpu["value"], "unit": UNIT,
+            "n_gpus": args.gpus, "steps": 1, "warmup": 0, "ms_per_step": None,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic", "config": config, "cpu_baseline": cpu,
+            "e2e": {"value": cpu["value"], "unit": UNIT, "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": 0}}), flush=True)
+        return
+
+    plan = thmm.Plan(parents)
+    device = local_rank
+    torch.cuda.set_device(device)
+    ws = thmm.Workspace()
+    ws.reserve_categorical_marginals(plan, K, B, K, observed, device, scalar=np.float32)
+    staged = ws.categorical_inputs(B)
+    staged.root_potential[:] = root
+    staged.emission_potentials[:] = emission
+    staged.edge_potentials[:] = edges
+    staged.observations[:] = observations
+    first = ws.posterior_marginals_prepared(staged, thmm.CategoricalInputUpdate.kAll)
+    log_z = np.array(first.log_partitions, dtype=np.float64)
+    rel = max(abs(log_z[b] - oracle_z[b]) / max(1.0, abs(oracle_z[b])) for b in range(sample))
+
+    ext = torch.cuda.ExternalStream(ws.stream, device=device)
+    for _ in range(args.warmup):
+        ws.enqueue(4)
+    torch.cuda.synchronize(device)
+    if dist is not None:
+        dist.barrier()
+    sampler = ClockSampler(device)
+    with sampler:
+        begin = torch.cuda.Event(enable_timing=True)
+        end = torch.cuda.Event(enable_timing=True)
+        begin.record(ext)
+        for _ in range(args.steps):
+            ws.enqueue(4)
+        end.record(ext)
+        end.synchronize()
+    launches = ws.launches
+    step_ms = reduce_max(begin.elapsed_time(end), dist) / args.steps
+    value = B * n * world / (step_ms / 1e3)
+
+    e2e_steps = args.e2e_steps or 5
+    calls = []
+    for _ in range(e2e_steps):
+        torch.cuda.synchronize(device)
+        t0 = time.perf_counter()
+        ws.posterior_marginals_prepared(staged, thmm.CategoricalInputUpdate.kAll)
+        calls.append(time.perf_counter() - t0)
+    e2e_total = reduce_max(sum(calls), dist)
+
+    S = 4
+    edge_bytes = e * K * K * S
+    algorithmic = (edge_bytes + B * leaves + B * (n * K + e * K * K) * S + B * S)
+    peaks = json.loads((ROOT / "MEASURED_PEAKS.json").read_text()) \
+        if (ROOT / "MEASURED_PEAKS.json").exists() else {}
+    peak = peaks.get("hbm_gbs", 6800.0)
+    achieved = algorithmic / (step_ms / 1e3) / 1e9
+    line = {
+        "metric": metric, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": step_ms, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {**config, "tuning": ws.tuning,
+                   "edge_bytes_read": edge_bytes,
+                   "edge_bytes_per_site_layout": B * edge_bytes,
+                   "log_z_max_rel_error_vs_fp64_oracle": rel, "checked_sites": sample,
+                   "l2": "outputs larger than L2 (node and edge marginals of every site)"},
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                     "frac": achieved / peak, "peak_source": "measured" if peaks else "fallback",
+                     "traffic": None, "algorithmic_bytes_per_launch": algorithmic},
+        "e2e": {"value": B * n * world * e2e_steps / e2e_total, "unit": UNIT,
+                "h2d_bytes_per_step": B * leaves + (K + K * K) * S + edge_bytes,
+                "d2h_bytes_per_step": B * S + B * (n * K + e * K * K) * S + 16,
+                "call_ms": [round(1e3 * c, 3) for c in calls]},
+        "gpu_launches": launches * args.steps,
+        "clocks": sampler.summary(),
+        "cpu_baseline": cpu,
+    }
     if rank == 0:
         print(json.dumps(line), flush=True)
 
