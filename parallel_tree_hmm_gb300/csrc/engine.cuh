@@ -172,6 +172,24 @@ __device__ __forceinline__ void LoadRow(const Src *p, unsigned K, Dst (&out)[KMA
       return;
     }
   }
+  if constexpr (KMAX > 4 && KMAX % 4 == 0 && sizeof(Src) == 4) {
+    // Rows of K % 4 == 0 floats start on 16-byte boundaries: quads.
+    if (K % 4 == 0 && (reinterpret_cast<std::uintptr_t>(p) & 15u) == 0) {
+#pragma unroll
+      for (unsigned q = 0; q < KMAX / 4; ++q) {
+        if (4 * q < K) {
+          const float4 v = reinterpret_cast<const float4 *>(p)[q];
+          out[4 * q] = static_cast<Dst>(v.x);
+          out[4 * q + 1] = static_cast<Dst>(v.y);
+          out[4 * q + 2] = static_cast<Dst>(v.z);
+          out[4 * q + 3] = static_cast<Dst>(v.w);
+        } else {
+          out[4 * q] = out[4 * q + 1] = out[4 * q + 2] = out[4 * q + 3] = Dst(0);
+        }
+      }
+      return;
+    }
+  }
 #pragma unroll
   for (unsigned j = 0; j < KMAX; ++j)
     out[j] = j < K ? static_cast<Dst>(p[j]) : Dst(0);
@@ -193,6 +211,17 @@ __device__ __forceinline__ void StoreRow(Dst *p, unsigned K, const Src (&in)[KMA
           make_double2(static_cast<double>(in[0]), static_cast<double>(in[1]));
       reinterpret_cast<double2 *>(p)[1] =
           make_double2(static_cast<double>(in[2]), static_cast<double>(in[3]));
+      return;
+    }
+  }
+  if constexpr (KMAX > 4 && KMAX % 4 == 0 && sizeof(Dst) == 4) {
+    if (K % 4 == 0 && (reinterpret_cast<std::uintptr_t>(p) & 15u) == 0) {
+#pragma unroll
+      for (unsigned q = 0; q < KMAX / 4; ++q)
+        if (4 * q < K)
+          reinterpret_cast<float4 *>(p)[q] =
+              make_float4(static_cast<float>(in[4 * q]), static_cast<float>(in[4 * q + 1]),
+                          static_cast<float>(in[4 * q + 2]), static_cast<float>(in[4 * q + 3]));
       return;
     }
   }
