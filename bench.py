@@ -81,6 +81,10 @@ def parse_args():
     parser.add_argument("--phase-rounds", type=int, default=None,
                         help="forest workload with --no-autotune: grid-wide rounds of the "
                              "phase schedule (0 automatic)")
+    parser.add_argument("--partition", action="store_true",
+                        help="forest workload under torchrun: the ranks share ONE forest, "
+                             "trees partitioned by node count (strong scaling), instead of "
+                             "one replica per rank (weak scaling)")
     parser.add_argument("--no-autotune", action="store_true",
                         help="forest and gw workloads: keep the default launch tuning "
                              "(a short run, e.g. under a profiler)")
@@ -139,6 +143,17 @@ class Forest:
         self.total_observed = int(sum(len(o) for o in self.observed))
         self.rng = rng
         self.cpu_plans = {}  # tree -> oracle planner plan (CPU legs)
+
+    def take(self, trees):
+        """The forest restricted to `trees` (indices, in order)."""
+        self.parents = [self.parents[t] for t in trees]
+        self.observed = [self.observed[t] for t in trees]
+        self.num_nodes = np.array([len(p) for p in self.parents], dtype=np.int64)
+        self.total_nodes = int(self.num_nodes.sum())
+        self.total_edges = int((self.num_nodes - 1).sum())
+        self.total_observed = int(sum(len(o) for o in self.observed))
+        self.cpu_plans = {}
+        return self
 
     def factors(self, seed: int):
         """One kFactors draw: root, emission and edge factors (float32)."""
@@ -316,6 +331,19 @@ def reduce_max(value, dist):
     return float(tensor.item())
 
 
+def reduce_sum(value, dist):
+    """Sum of `value` over all ranks."""
+    if dist is None:
+        return value
+    import torch
+
+    on_gpu = dist.get_backend() == "nccl"
+    tensor = torch.tensor([float(value)], dtype=torch.float64,
+                          device="cuda" if on_gpu else "cpu")
+    dist.all_reduce(tensor, op=dist.ReduceOp.SUM)
+    return float(tensor.item())
+
+
 def rank_seed(seed: int, rank: int) -> int:
     """Each rank contracts its own forest replica (weak scaling, no
     collective on the data path); replicas differ only by seed."""
@@ -369,7 +397,13 @@ def run_ours(args, rank, world, local_rank, dist):
 
     device = local_rank
     torch.cuda.set_device(device)
-    forest = Forest(args.trees, args.states, rank_seed(args.seed, rank))
+    if args.partition:
+        from parallel_tree_hmm_gb300 import sharding
+
+        forest = Forest(args.trees, args.states, args.seed)
+        forest.take(sharding.partition_trees(forest.num_nodes, world)[rank])
+    else:
+        forest = Forest(args.trees, args.states, rank_seed(args.seed, rank))
     K = forest.states
     setup_start = time.perf_counter()
     plans = thmm.Plan.many(forest.parents)
@@ -434,7 +468,12 @@ def run_ours(args, rank, world, local_rank, dist):
     launches_per_step = ws.launches
     elapsed_ms = reduce_max(elapsed_ms, dist)
     launch_ms = elapsed_ms / args.steps
-    value = nodes_done * world / (elapsed_ms / 1e3)
+    # Replicas: every rank contracts its own forest of the same size; a
+    # partitioned forest: the ranks' shares add up to one forest.
+    all_nodes = (int(reduce_sum(forest.total_nodes, dist)) if args.partition
+                 else forest.total_nodes * world)
+    value = (reduce_sum(nodes_done, dist) if args.partition else nodes_done * world) / (
+        elapsed_ms / 1e3)
 
     # Plain FP64 arithmetic on the same inputs.
     ws64 = reserve(np.float64)
@@ -447,7 +486,8 @@ def run_ours(args, rank, world, local_rank, dist):
                                    / np.maximum(1.0, np.abs(plain.log_partitions))))
     plain_steps = max(2, args.steps // 4)
     plain_ms, plain_nodes = device_time(ws64, plain_steps, 1)
-    plain_value = plain_nodes * world / (reduce_max(plain_ms, dist) / 1e3)
+    plain_value = (reduce_sum(plain_nodes, dist) if args.partition else plain_nodes * world) / (
+        reduce_max(plain_ms, dist) / 1e3)
     del ws64, staged64, plain
 
     # End to end through the prepared call: pinned staging -> H2D -> kernel -> D2H.
@@ -472,7 +512,7 @@ def run_ours(args, rank, world, local_rank, dist):
         api_download_ms.append(result.timings.download_ms)
         api_wall_ms.append(result.timings.wall_ms)
     e2e_total = reduce_max(e2e_total, dist)
-    e2e_value = forest.total_nodes * world * e2e_steps / e2e_total
+    e2e_value = all_nodes * e2e_steps / e2e_total
     S = 4
     h2d = forest.total_edges * K * K * S + (K + K * K) * S
     d2h = len(plans) * S + forest.total_nodes * K * S + forest.total_edges * K * K * S + 16
@@ -490,12 +530,21 @@ def run_ours(args, rank, world, local_rank, dist):
         if key in info:
             traffic = info[key]["bytes_per_node"] * forest.total_nodes
 
+    partition = {}
+    if args.partition:
+        from parallel_tree_hmm_gb300 import sharding
+
+        partition = {"parallelism": f"one forest partitioned by node count over {world} GPUs",
+                     "trees": args.trees, "nodes_all_ranks": all_nodes,
+                     "nodes_this_rank": forest.total_nodes,
+                     "sum_log_partition_all_ranks": sharding.sum_log_partitions(
+                         log_z_reference, dist)}
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": launch_ms,
-        "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-        "dtype": "f32", "data": "synthetic",
-        "config": {**workload_config(args, forest),
+        "higher_is_better": True, "scaling": "strong" if args.partition else "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {**workload_config(args, forest), **partition,
                    "plain_fp64_nodes_per_s": plain_value,
                    "chosen_over_plain_fp64": value / plain_value,
                    "plain_fp64_log_z_rel_diff": plain_logz_diff,
