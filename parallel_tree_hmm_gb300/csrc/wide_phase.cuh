@@ -1,8 +1,9 @@
 // Phase kernels of the level-synchronous schedule (phase.h) for 32 < K <= 128
 // states: round r of EVERY tree in one grid-wide launch per kind, as for
-// K <= 4, but one operation per CTA of 128 threads (rakes: warp-per-row
-// K x K matrix-vector products; compressions and their adjoints: tcgen05
-// products with TMEM accumulators, as the per-tree tensor-core engine).
+// K <= 4, but one operation per CTA (128 threads at K_P = 64, 256 at 128;
+// rakes: warp-per-row K x K matrix-vector products; compressions and their
+// adjoints: tcgen05 products with TMEM accumulators, as the per-tree
+// tensor-core engine).
 //
 // The per-tree engine (wide_engine.cuh) contracts one tree per CTA, so a
 // forest of 16 trees keeps 16 SMs busy and each SM runs one operation at a
@@ -84,6 +85,8 @@ struct PhaseShared {
 };
 
 template <unsigned T> __device__ __forceinline__ float CtaMax(float v, PhaseShared &sh) {
+  static_assert(T % 32 == 0 && T / 32 <= sizeof(PhaseShared::reduce) / sizeof(float),
+                "one reduction slot per warp");
   v = WarpMax(v);
   if ((threadIdx.x & 31) == 0)
     sh.reduce[threadIdx.x / 32] = v;
