@@ -6,7 +6,11 @@
 //   2. a double-precision host run of the phase records, launch range by
 //      launch range (whole batch, cut into instance stripes through
 //      PhasePlan::OpRange, and with the last rounds taken from the per-tree
-//      tail records), reproduces the oracle's log Z and marginals.
+//      tail records), reproduces the oracle's log Z and marginals, both with
+//      the adjoint of a compression recomputing its product (the K <= 32
+//      kernels) and with it reading the stored compressed path and its own
+//      scale, comp_scale minus its inputs' scales (the tensor-core phase
+//      kernels, wide_phase.cuh).
 #include <algorithm>
 #include <cmath>
 #include <cstdint>
@@ -106,6 +110,7 @@ struct HostRun {
   std::vector<double> nodes, node_scale, comps, comp_scale, comp_mu;
   std::vector<double> values, node_out, edge_out;
   std::vector<int> edge_uses, comp_writes, comp_reads;
+  bool stored_ratio = false; // adjoint ratio from the stored compressed path
 
   void Input(std::uint32_t node, double *out) const {
     for (std::size_t j = 0; j < K; ++j)
@@ -247,15 +252,24 @@ struct HostRun {
   void CompressReverse(std::uint32_t i) {
     const thmm::Uint4 op = compress[i];
     std::vector<double> middle(K), ratio(K * K, 0.0), row(K), mid_adj(K, 0.0);
-    double unused = 0;
-    Node(op.y, middle.data(), unused);
+    double inputs = Scale(op.x) + Scale(op.z);
+    Node(op.y, middle.data(), inputs);
     const double *left = Path(op.x), *right = Path(op.z);
-    for (std::size_t p = 0; p < K; ++p)
-      for (std::size_t m = 0; m < K; ++m)
-        for (std::size_t c = 0; c < K; ++c)
-          ratio[p * K + c] += left[p * K + m] * middle[m] * right[m * K + c];
-    for (std::size_t j = 0; j < K * K; ++j)
-      ratio[j] = ratio[j] > 0 ? comp_mu[i * K * K + j] / ratio[j] : 0;
+    if (stored_ratio) {
+      // product = stored path * exp(own scale); ratio = mu / product.
+      const double own = comp_scale[i] - inputs;
+      for (std::size_t j = 0; j < K * K; ++j) {
+        const double stored = comps[i * K * K + j];
+        ratio[j] = stored > 0 ? comp_mu[i * K * K + j] / stored * std::exp(-own) : 0;
+      }
+    } else {
+      for (std::size_t p = 0; p < K; ++p)
+        for (std::size_t m = 0; m < K; ++m)
+          for (std::size_t c = 0; c < K; ++c)
+            ratio[p * K + c] += left[p * K + m] * middle[m] * right[m * K + c];
+      for (std::size_t j = 0; j < K * K; ++j)
+        ratio[j] = ratio[j] > 0 ? comp_mu[i * K * K + j] / ratio[j] : 0;
+    }
     for (std::size_t p = 0; p < K; ++p) {
       for (std::size_t m = 0; m < K; ++m) {
         double dot = 0;
@@ -387,10 +401,11 @@ void CheckForest(std::mt19937_64 &rng, bool shared_edges, std::size_t K, int str
   for (double &v : edge_in)
     v = rng() % 17 == 0 ? 0.0 : u(rng);
 
-  // 2. Host run: whole batch, striped, and with tails from rounds 1 and 2.
-  for (int pass = 0; pass < 4; ++pass) {
+  // 2. Host run: whole batch, striped, with tails from rounds 1 and 2, and
+  //    (pass 4) striped with the stored-path adjoint ratio.
+  for (int pass = 0; pass < 5; ++pass) {
     const std::uint32_t grid_rounds =
-        pass < 2 ? plan.rounds : static_cast<std::uint32_t>(pass - 1);
+        pass < 2 || pass == 4 ? plan.rounds : static_cast<std::uint32_t>(pass - 1);
     const thmm::PhasePlan::Tail tail =
         grid_rounds < plan.rounds ? plan.BuildTail(grid_rounds) : thmm::PhasePlan::Tail{};
     HostRun run{plan, plan.rakes, plan.gathers, plan.compress, plan.roots, K, node_in, edge_in,
@@ -406,6 +421,7 @@ void CheckForest(std::mt19937_64 &rng, bool shared_edges, std::size_t K, int str
     run.edge_uses.assign(edges, 0);
     run.comp_writes.assign(comps, 0);
     run.comp_reads.assign(comps, 0);
+    run.stored_ratio = pass == 4;
     const int parts = pass == 0 ? 1 : stripes;
     for (int s = 0; s < parts; ++s)
       run.Run(static_cast<std::uint32_t>(batch * s / parts),
@@ -444,7 +460,7 @@ void CheckForest(std::mt19937_64 &rng, bool shared_edges, std::size_t K, int str
 
 int main() {
   std::mt19937_64 rng(11);
-  for (std::size_t K : {1, 3, 4}) {
+  for (std::size_t K : {1, 3, 4, 7}) {
     CheckForest(rng, false, K, 3);
     CheckForest(rng, true, K, 4);
   }
