@@ -96,9 +96,11 @@ def parse_args():
                         default="forest",
                         help="forest: uneven forest, marginals (default); gw: "
                              "Galton-Watson forest, MAP + posterior sampling; dense: "
-                             "spine-heavy trees, K = 64 or 128, tensor-core marginals")
+                             "spine-heavy trees, K = 64 or 128, tensor-core marginals; "
+                             "sites: the batch API on one binary tree with many sites")
     parser.add_argument("--tree-nodes", type=int, default=None,
-                        help="dense workload: nodes per tree")
+                        help="dense workload: nodes per tree; sites workload: nodes of "
+                             "the tree (default 2001)")
     parser.add_argument("--shape", choices=["spine-heavy", "recursive"], default="spine-heavy",
                         help="dense workload: tree shape")
     parser.add_argument("--edge-sigma", type=float, default=2.0,
